@@ -1,0 +1,145 @@
+/*
+ * qhmat_gb300 -- C ABI of the GB300-resident quantized H-matrix matvec.
+ *
+ * Plain C types only (pointers, sizes, ints); no torch or C++ types cross this
+ * boundary.  Every entry point returns an int status (QH_OK on success) and
+ * records a message for the calling thread, read back with qh_last_error().
+ * Status codes map onto the exception types the reference raises through
+ * pybind11: QH_EINVAL -> ValueError (std::invalid_argument), QH_ERUNTIME and
+ * QH_ECUDA -> RuntimeError (std::runtime_error), QH_EOVERFLOW -> OverflowError
+ * (std::overflow_error).
+ *
+ * What each entry replaces in inEXASCALE/qhmat:
+ *   qh_matrix_from_qhmat  HMatrix::load (src/qhmat/io.cpp:173-257) plus the
+ *                         per-call flatten + upload of HMatrix::matmul_cuda
+ *                         (src/qhmat/cuda.cu:119-150), done once.
+ *   qh_matrix_from_arrays the flattened arrays HMatrix::matmul_cuda builds on
+ *                         every call (src/qhmat/cuda.cu:119-141), handed over
+ *                         once; DeviceBlock (src/qhmat/cuda.cu:42-46) is
+ *                         qh_block_desc below.
+ *   qh_matmul_host        std::vector<double> HMatrix::matmul_cuda(x, rhs)
+ *                         (src/qhmat/core.hpp:64-65, src/qhmat/cuda.cu:106-164):
+ *                         host x in, host y out, same validation and messages.
+ *   qh_matmul_device      the device-resident form of the same apply: x and y
+ *                         are device pointers, stream-ordered, no host sync.
+ *   qh_cuda_built         the module attribute qhmat.cuda_built
+ *                         (src/qhmat/bindings.cpp:200-204).
+ *
+ * Layout of x and y (both entries): row-major order x rhs in SOURCE index
+ * order, x[i*rhs + p], exactly as HMatrix::matmul takes and returns them
+ * (src/qhmat/core.cpp:360-390).
+ */
+#ifndef QHMAT_GB300_H
+#define QHMAT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define QH_API __attribute__((visibility("default")))
+#else
+#define QH_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define QH_OK 0
+#define QH_EINVAL 1    /* ValueError    (std::invalid_argument in the reference) */
+#define QH_ERUNTIME 2  /* RuntimeError  (std::runtime_error) */
+#define QH_EOVERFLOW 3 /* OverflowError (std::overflow_error) */
+#define QH_ECUDA 4     /* RuntimeError raised from a CUDA runtime failure */
+
+typedef struct qh_matrix qh_matrix;
+
+/* Mirrors DeviceBlock (src/qhmat/cuda.cu:42-46): one block of the partition in
+ * clustered coordinates.  factor_offset indexes the per-component arrays
+ * (widths, scales, offsets); dense_offset indexes the dense value array. */
+typedef struct {
+    size_t row0, row1, col0, col1;
+    size_t rank, factor_offset, dense_offset;
+    int is_dense;
+} qh_block_desc;
+
+/* Size figures of a resident matrix (all in bytes unless named otherwise).
+ * model_bytes is the packed-byte traffic model of one single-RHS apply:
+ * 4*(left+right code words) + 16*sum(rank) + 8*sum(dense m*n) + 16*order. */
+typedef struct {
+    uint64_t order, block_count, dense_blocks, lowrank_blocks, components;
+    uint64_t code_bytes;      /* 4 * (left + right code words), as stored by the reference */
+    uint64_t scale_bytes;     /* 16 * sum(rank): one left and one right FP64 scale each */
+    uint64_t dense_bytes;     /* 8 * sum over dense blocks of m*n */
+    uint64_t model_bytes;     /* code + scale + dense + 16*order (x read, y written) */
+    uint64_t device_bytes;    /* bytes the resident layout occupies on the device */
+    uint64_t row_tiles;       /* row-side work units */
+    uint64_t flops_per_rhs;   /* 2*(sum rank*(m+n) + sum dense m*n) */
+} qh_stats;
+
+/* Message of the last failing call made by this thread ("" if none). */
+QH_API const char* qh_last_error(void);
+
+/* 1: this library applies on CUDA devices (mirrors qhmat.cuda_built). */
+QH_API int qh_cuda_built(void);
+
+/* Parse and validate a QHMAT001 image with the reference's checks and
+ * messages, build the resident layout, and upload it to `device` (one
+ * cudaMalloc'd arena owned by the handle). */
+QH_API int qh_matrix_from_qhmat(const void* bytes, size_t len, int device, qh_matrix** out);
+
+/* Same, from the arrays HMatrix::matmul_cuda flattens (cuda.cu:119-141):
+ * permutation[order]; blocks[block_count]; dense values concatenated in block
+ * order; left/right words concatenated in block order with per-component
+ * offsets already rebased onto those arrays; scales and widths per component.
+ * The partition is validated as HMatrix::finalize does (core.cpp:332-358). */
+QH_API int qh_matrix_from_arrays(size_t order, const size_t* permutation, size_t block_count,
+                          const qh_block_desc* blocks, const double* dense,
+                          const uint32_t* left_words, const uint32_t* right_words,
+                          const size_t* left_offsets, const size_t* right_offsets,
+                          const double* left_scales, const double* right_scales,
+                          const int* widths, int device, qh_matrix** out);
+
+QH_API void qh_matrix_destroy(qh_matrix* m);
+
+QH_API int qh_matrix_stats(const qh_matrix* m, qh_stats* out);
+
+/* Max-norm bound of the stored matrix (HMatrix::reconstruction_bound,
+ * src/qhmat/core.cpp:467-472). */
+QH_API double qh_matrix_reconstruction_bound(const qh_matrix* m);
+
+/* Device scratch (bytes) one qh_matmul_device call with `rhs` columns needs. */
+QH_API size_t qh_workspace_bytes(const qh_matrix* m, size_t rhs);
+
+/* y = A x on the device.  x, y: device pointers, row-major order x rhs, source
+ * order.  workspace: device scratch of at least qh_workspace_bytes(m, rhs)
+ * bytes, 256-byte aligned, not shared with a concurrent call; NULL uses a
+ * buffer the handle allocates on first use.  stream: a cudaStream_t (NULL =
+ * legacy default stream).  status: optional device int that the call sets to 1
+ * when x holds a NaN or infinity (and leaves untouched otherwise); y is then
+ * unspecified.  Stream-ordered: returns once the work is enqueued. */
+QH_API int qh_matmul_device(const qh_matrix* m, const double* x, double* y, size_t rhs,
+                     void* workspace, size_t workspace_bytes, void* stream, int* status);
+
+/* Drop-in for HMatrix::matmul_cuda: host x (order*rhs doubles), host y.
+ * Copies x in through pinned staging, applies, copies y back and
+ * synchronises.  Raises the reference's errors: "right-hand-side shape
+ * mismatch", "nonfinite right-hand side" (QH_EINVAL), "CUDA launch grid too
+ * large" (QH_EOVERFLOW), "no CUDA device is available" (QH_ERUNTIME). */
+QH_API int qh_matmul_host(const qh_matrix* m, const double* x, double* y, size_t rhs);
+
+/* Validation aid: decode every stored code of one factor side on the device
+ * with the same device routine the apply kernels use, and copy the integers
+ * to host `out`, component-major in block order (component c of a block with
+ * `rows` entries on that side fills rows consecutive ints).  side 0 = left /
+ * P (block rows), side 1 = right / Q (block columns).  `out_count` must equal
+ * the total number of codes on that side (returned through `needed` when out
+ * is NULL).  No reference counterpart: it exposes HMatrix::decode
+ * (src/qhmat/core.cpp:269-282) semantics of the resident layout for tests. */
+QH_API int qh_debug_decode(const qh_matrix* m, int side, int32_t* out, size_t out_count,
+                           size_t* needed);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* QHMAT_GB300_H */

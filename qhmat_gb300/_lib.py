@@ -1,0 +1,84 @@
+"""ctypes binding of ``libqhmat_gb300.so`` (the C ABI in include/qhmat_gb300.h).
+
+The library is the only compute path: if it is missing or fails to load, every
+entry point raises instead of falling back to anything else.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "libqhmat_gb300.so"
+
+QH_OK, QH_EINVAL, QH_ERUNTIME, QH_EOVERFLOW, QH_ECUDA = 0, 1, 2, 3, 4
+
+
+class QhStats(C.Structure):
+    _fields_ = [(name, C.c_uint64) for name in (
+        "order", "block_count", "dense_blocks", "lowrank_blocks", "components", "code_bytes",
+        "scale_bytes", "dense_bytes", "model_bytes", "device_bytes", "row_tiles", "flops_per_rhs")]
+
+
+class QhBlockDesc(C.Structure):
+    _fields_ = [("row0", C.c_size_t), ("row1", C.c_size_t), ("col0", C.c_size_t),
+                ("col1", C.c_size_t), ("rank", C.c_size_t), ("factor_offset", C.c_size_t),
+                ("dense_offset", C.c_size_t), ("is_dense", C.c_int)]
+
+
+_lib = None
+
+
+def load_library() -> C.CDLL:
+    """Load the in-tree CUDA library (building it first if QHMAT_GB300_BUILD=1)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if os.environ.get("QHMAT_GB300_BUILD") == "1" or not LIB_PATH.exists():
+        from . import build as _build
+
+        try:
+            _build.build()
+        except Exception as exc:  # noqa: BLE001 - re-raised with context
+            raise RuntimeError(f"qhmat_gb300 CUDA library is not built and building it failed: {exc}")
+    lib = C.CDLL(str(LIB_PATH))
+    vp, sz, i32 = C.c_void_p, C.c_size_t, C.c_int
+    lib.qh_last_error.restype = C.c_char_p
+    lib.qh_last_error.argtypes = []
+    lib.qh_cuda_built.restype = i32
+    lib.qh_cuda_built.argtypes = []
+    lib.qh_matrix_from_qhmat.restype = i32
+    lib.qh_matrix_from_qhmat.argtypes = [C.c_char_p, sz, i32, C.POINTER(vp)]
+    lib.qh_matrix_from_arrays.restype = i32
+    lib.qh_matrix_from_arrays.argtypes = [sz, vp, sz, vp, vp, vp, vp, vp, vp, vp, vp, vp, i32,
+                                          C.POINTER(vp)]
+    lib.qh_matrix_destroy.restype = None
+    lib.qh_matrix_destroy.argtypes = [vp]
+    lib.qh_matrix_stats.restype = i32
+    lib.qh_matrix_stats.argtypes = [vp, C.POINTER(QhStats)]
+    lib.qh_matrix_reconstruction_bound.restype = C.c_double
+    lib.qh_matrix_reconstruction_bound.argtypes = [vp]
+    lib.qh_workspace_bytes.restype = sz
+    lib.qh_workspace_bytes.argtypes = [vp, sz]
+    lib.qh_matmul_device.restype = i32
+    lib.qh_matmul_device.argtypes = [vp, vp, vp, sz, vp, sz, vp, vp]
+    lib.qh_matmul_host.restype = i32
+    lib.qh_matmul_host.argtypes = [vp, vp, vp, sz]
+    lib.qh_debug_decode.restype = i32
+    lib.qh_debug_decode.argtypes = [vp, i32, vp, sz, C.POINTER(sz)]
+    _lib = lib
+    return lib
+
+
+def raise_for(code: int) -> None:
+    """Map a QH_* status to the exception type the reference raises."""
+    if code == QH_OK:
+        return
+    msg = load_library().qh_last_error().decode(errors="replace")
+    if code == QH_EINVAL:
+        raise ValueError(msg)
+    if code == QH_EOVERFLOW:
+        raise OverflowError(msg)
+    raise RuntimeError(msg)

@@ -1,0 +1,211 @@
+"""GPU-resident drop-in for the reference's quantized H-matrix apply.
+
+Mirrors ``qhmat.HMatrix.matmul(x, *, device="cuda")`` (python/qhmat/matrix.py:
+295-303) and ``NativeHMatrix.matmul(x, use_cuda)`` (src/qhmat/bindings.cpp:
+152-179): same argument meaning, same shape rules, same exception types and
+messages.  The difference is residency: the representation is uploaded once
+when the object is created, and every ``matmul`` only moves x and y.
+
+Inputs may be NumPy arrays (host path: one pinned copy in and one copy out per
+call, through ``qh_matmul_host``) or CUDA ``torch.float64`` tensors (device
+path: zero-copy, stream-ordered, through ``qh_matmul_device``; the result is a
+CUDA tensor).  Only the GPU applies: ``device="cpu"`` is rejected rather than
+served by a CPU fallback.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+from ._lib import QhBlockDesc, QhStats, load_library, raise_for
+
+
+def _torch():
+    import torch
+
+    return torch
+
+
+def _is_torch_tensor(x) -> bool:
+    mod = type(x).__module__
+    return mod.startswith("torch") and hasattr(x, "is_cuda")
+
+
+class HMatrix:
+    """A quantized H-matrix resident on one CUDA device."""
+
+    def __init__(self, handle: int, device: int):
+        self._lib = load_library()
+        self._h = C.c_void_p(handle)
+        self._device = device
+        st = QhStats()
+        raise_for(self._lib.qh_matrix_stats(self._h, C.byref(st)))
+        self._stats = {name: int(getattr(st, name)) for name, _ in QhStats._fields_}
+
+    # ------------------------------------------------------------ creation
+    @classmethod
+    def from_bytes(cls, data: bytes, *, device: int = 0) -> "HMatrix":
+        """Parse and upload a QHMAT001 image (the reference's file format)."""
+        lib = load_library()
+        out = C.c_void_p()
+        raise_for(lib.qh_matrix_from_qhmat(bytes(data), len(data), device, C.byref(out)))
+        return cls(out.value, device)
+
+    @classmethod
+    def load(cls, path: str | os.PathLike[str], *, device: int = 0) -> "HMatrix":
+        """Load a file written by the reference's ``HMatrix.save``."""
+        return cls.from_bytes(Path(path).read_bytes(), device=device)
+
+    @classmethod
+    def from_reference(cls, matrix, *, device: int = 0) -> "HMatrix":
+        """Upload a reference ``qhmat.HMatrix`` / ``NativeHMatrix`` via its own ``save``."""
+        import tempfile
+
+        with tempfile.TemporaryDirectory() as d:
+            path = Path(d) / "matrix.qhmat"
+            matrix.save(str(path))
+            return cls.load(path, device=device)
+
+    @classmethod
+    def from_arrays(cls, order, permutation, blocks, dense, left_words, right_words,
+                    left_offsets, right_offsets, left_scales, right_scales, widths, *,
+                    device: int = 0) -> "HMatrix":
+        """Create from the flat arrays the reference's CUDA path builds per call.
+
+        ``blocks`` is a sequence of (row0, row1, col0, col1, rank, factor_offset,
+        dense_offset, is_dense) tuples (DeviceBlock, src/qhmat/cuda.cu:42-46).
+        """
+        lib = load_library()
+        perm = np.ascontiguousarray(permutation, dtype=np.uintp)
+        descs = (QhBlockDesc * len(blocks))(*[QhBlockDesc(*map(int, b)) for b in blocks])
+        arrs = [np.ascontiguousarray(dense, np.float64), np.ascontiguousarray(left_words, np.uint32),
+                np.ascontiguousarray(right_words, np.uint32),
+                np.ascontiguousarray(left_offsets, np.uintp),
+                np.ascontiguousarray(right_offsets, np.uintp),
+                np.ascontiguousarray(left_scales, np.float64),
+                np.ascontiguousarray(right_scales, np.float64), np.ascontiguousarray(widths, np.intc)]
+        out = C.c_void_p()
+        raise_for(lib.qh_matrix_from_arrays(order, perm.ctypes.data, len(blocks), C.addressof(descs),
+                                            *[a.ctypes.data for a in arrs], device, C.byref(out)))
+        return cls(out.value, device)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and self._h.value:
+            self._lib.qh_matrix_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001 - interpreter shutdown
+            pass
+
+    # ------------------------------------------------------------ metadata
+    @property
+    def order(self) -> int:
+        return self._stats["order"]
+
+    @property
+    def shape(self) -> tuple[int, int]:
+        return self.order, self.order
+
+    @property
+    def device(self) -> int:
+        return self._device
+
+    @property
+    def reconstruction_bound(self) -> float:
+        """Max-norm bound of the stored matrix (as the reference reports it)."""
+        return float(self._lib.qh_matrix_reconstruction_bound(self._h))
+
+    @property
+    def stats(self) -> dict:
+        """Block counts and the packed-byte traffic model of one apply."""
+        return dict(self._stats)
+
+    def model_bytes(self, rhs: int = 1) -> int:
+        """Packed-byte traffic model of one apply with ``rhs`` columns."""
+        s = self._stats
+        return s["code_bytes"] + s["scale_bytes"] + s["dense_bytes"] + 16 * s["order"] * rhs
+
+    def workspace_bytes(self, rhs: int = 1) -> int:
+        return int(self._lib.qh_workspace_bytes(self._h, rhs))
+
+    # ------------------------------------------------------------ apply
+    def _check_shape(self, shape) -> int:
+        if len(shape) not in (1, 2):
+            raise ValueError("right-hand side must be one- or two-dimensional")
+        if shape[0] != self.order:
+            raise ValueError("right-hand side has the wrong row count")
+        return 1 if len(shape) == 1 else int(shape[1])
+
+    def matmul(self, x, *, device: str = "cuda", stream=None, workspace=None, check: bool = True):
+        """Apply to an ``(n,)`` vector or ``(n, p)`` array in FP64 on the GPU.
+
+        NumPy input returns a new NumPy array; a CUDA float64 torch tensor
+        returns a CUDA tensor computed on ``stream`` (default: torch's current
+        stream).  ``check=False`` skips the device-side nonfinite check's host
+        synchronisation on the tensor path.
+        """
+        if device not in ("cpu", "cuda"):
+            raise ValueError("device must be 'cpu' or 'cuda'")
+        if device != "cuda":
+            raise ValueError("qhmat_gb300 applies on the GPU only; use device='cuda'")
+        if _is_torch_tensor(x):
+            return self._matmul_tensor(x, stream=stream, workspace=workspace, check=check)
+        a = np.ascontiguousarray(np.asarray(x, dtype=np.float64))
+        rhs = self._check_shape(a.shape)
+        y = np.empty_like(a)
+        raise_for(self._lib.qh_matmul_host(self._h, a.ctypes.data, y.ctypes.data, rhs))
+        return y
+
+    def _matmul_tensor(self, x, *, stream=None, workspace=None, check=True):
+        torch = _torch()
+        if not x.is_cuda or x.device.index != self._device:
+            raise ValueError(f"tensor right-hand side must live on cuda:{self._device}")
+        if x.dtype != torch.float64:
+            raise ValueError("tensor right-hand side must be torch.float64")
+        rhs = self._check_shape(tuple(x.shape))
+        x = x.contiguous()
+        y = torch.empty_like(x)
+        need = self.workspace_bytes(rhs)
+        if workspace is None:
+            workspace = torch.empty(need, dtype=torch.uint8, device=x.device)
+        elif workspace.numel() * workspace.element_size() < need:
+            raise ValueError("workspace too small")
+        status = torch.zeros(1, dtype=torch.int32, device=x.device)
+        s = stream if stream is not None else torch.cuda.current_stream(x.device)
+        raise_for(self._lib.qh_matmul_device(self._h, x.data_ptr(), y.data_ptr(), rhs,
+                                             workspace.data_ptr(), need, s.cuda_stream,
+                                             status.data_ptr()))
+        if check and int(status.item()):
+            raise ValueError("nonfinite right-hand side")
+        return y
+
+    def __matmul__(self, x):
+        return self.matmul(x)
+
+    def debug_decode(self, side: int) -> np.ndarray:
+        """All codes of one factor side decoded on the GPU (component-major)."""
+        need = C.c_size_t()
+        raise_for(self._lib.qh_debug_decode(self._h, side, None, 0, C.byref(need)))
+        out = np.empty(need.value, np.int32)
+        raise_for(self._lib.qh_debug_decode(self._h, side, out.ctypes.data, out.size, None))
+        return out
+
+
+class NativeHMatrix(HMatrix):
+    """Mirror of ``qhmat.NativeHMatrix.matmul(x, use_cuda)`` for the GPU apply."""
+
+    def matmul(self, x, use_cuda: bool = True, **kw):  # type: ignore[override]
+        if not use_cuda:
+            raise RuntimeError("qhmat_gb300 applies on the GPU only; pass use_cuda=True")
+        return super().matmul(x, device="cuda", **kw)
+
+
+def cuda_built() -> bool:
+    return bool(load_library().qh_cuda_built())

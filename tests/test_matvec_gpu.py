@@ -1,0 +1,149 @@
+"""GPU parity of the resident matvec against the reference (via its golden
+fixtures) and the CPU oracle.  Every call goes through the C ABI
+(libqhmat_gb300.so) -- there is no other compute path.
+
+Tolerance (stated by the build target): ||y - y_ref|| / ||y_ref|| <= 1e-13,
+with y_ref the reference's CPU HMatrix::matmul on identical inputs; code
+unpacking is compared bit-for-bit.
+"""
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN_CASES, golden, rel_err
+from oracle import oracle as O
+from qhmat_gb300 import HMatrix, NativeHMatrix
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-13
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_matmul_matches_reference(cuda_device, name):
+    data, g = golden(name)
+    h = HMatrix.from_bytes(data)
+    y = h.matmul(g["x"], device="cuda")
+    assert y.shape == g["y"].shape
+    assert rel_err(y, g["y"]) <= TOL
+    # column-wise too: every right-hand side on its own
+    x2 = g["x"] if g["x"].ndim == 2 else g["x"][:, None]
+    y2 = g["y"] if g["y"].ndim == 2 else g["y"][:, None]
+    for p in range(x2.shape[1]):
+        yp = h.matmul(np.ascontiguousarray(x2[:, p]))
+        assert yp.shape == (h.order,)
+        assert rel_err(yp, y2[:, p]) <= TOL
+    assert h.reconstruction_bound == float(g["bound"])
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_codes_round_trip_bit_exact(cuda_device, name):
+    """Codes decoded by the device routine == the reference decode, bit for bit."""
+    data, _ = golden(name)
+    h = HMatrix.from_bytes(data)
+    m = O.OracleMatrix(data)
+    for side in (0, 1):
+        expect = [m.codes(b, side).ravel() for b in range(m.block_count)
+                  if not m.block_info(b)["dense"]]
+        expect = np.concatenate(expect) if expect else np.zeros(0, np.int32)
+        got = h.debug_decode(side)
+        assert got.dtype == np.int32 and np.array_equal(got, expect)
+
+
+def test_tensor_path_matches_host_path_and_is_deterministic(cuda_device):
+    import torch
+
+    data, g = golden("cfg1")
+    h = HMatrix.from_bytes(data)
+    x = torch.from_numpy(g["x"]).cuda()
+    y1 = h.matmul(x)
+    y2 = h.matmul(x)
+    assert y1.is_cuda and y1.dtype == torch.float64
+    assert torch.equal(y1, y2), "two applies differ bitwise"
+    assert np.array_equal(y1.cpu().numpy(), h.matmul(g["x"]))
+    assert rel_err(y1.cpu().numpy(), g["y"]) <= TOL
+
+
+def test_random_rhs_against_oracle(cuda_device):
+    for name in ("ragged300", "cfg1"):
+        data, _ = golden(name)
+        h = HMatrix.from_bytes(data)
+        m = O.OracleMatrix(data)
+        rng = np.random.default_rng(99)
+        for shape in [(m.order,), (m.order, 1), (m.order, 7)]:
+            x = rng.standard_normal(shape)
+            assert rel_err(h.matmul(x), m.matmul(x, threads=4)) <= TOL
+        # graded magnitudes: entries spread over 2^-40 .. 2^40
+        x = rng.standard_normal(m.order) * np.exp2(rng.integers(-40, 40, m.order))
+        assert rel_err(h.matmul(x), m.matmul(x)) <= TOL
+        # zeros and a single spike
+        assert np.array_equal(h.matmul(np.zeros(m.order)), np.zeros(m.order))
+        e = np.zeros(m.order)
+        e[m.order // 3] = 1.0
+        assert rel_err(h.matmul(e), m.matmul(e)) <= TOL
+
+
+def test_errors_match_reference(cuda_device):
+    data, g = golden("cuda10")
+    h = HMatrix.from_bytes(data)
+    x = g["x"].copy()
+    x[2, 1] = np.inf
+    with pytest.raises(ValueError, match="nonfinite right-hand side"):
+        h.matmul(x)
+    with pytest.raises(ValueError, match="wrong row count"):
+        h.matmul(np.ones(11))
+    with pytest.raises(ValueError, match="one- or two-dimensional"):
+        h.matmul(np.ones((10, 2, 2)))
+    with pytest.raises(ValueError, match="device must be"):
+        h.matmul(g["x"], device="tpu")
+    # still usable after an error
+    assert rel_err(h.matmul(g["x"]), g["y"]) <= TOL
+    n = NativeHMatrix.from_bytes(data)
+    assert rel_err(n.matmul(g["x"], True), g["y"]) <= TOL
+
+
+def test_from_arrays_matches_file_path(cuda_device):
+    """The flat-array entry (the arrays matmul_cuda builds) gives the same result."""
+    data, g = golden("ragged300")
+    m = O.OracleMatrix(data)
+    import struct
+
+    blocks, dense, lw, rw, loff, roff, ls, rs, widths = [], [], [], [], [], [], [], [], []
+    off = 8 + 24
+    perm = np.frombuffer(data, np.uint64, m.order, off).astype(np.uintp)
+    off += 8 * m.order
+    dense_n = 0
+    for b in range(m.block_count):
+        info = m.block_info(b)
+        rows, cols = info["row1"] - info["row0"], info["col1"] - info["col0"]
+        off += 34
+        if info["dense"]:
+            blocks.append((info["row0"], info["row1"], info["col0"], info["col1"], 0, 0, dense_n, 1))
+            dense.append(np.frombuffer(data, np.float64, rows * cols, off))
+            dense_n += rows * cols
+            off += 8 * rows * cols
+            continue
+        rank = info["rank"]
+        off += 32
+        w = np.frombuffer(data, np.uint8, rank, off).astype(np.intc)
+        off += rank
+        lsc = np.frombuffer(data, np.float64, rank, off)
+        rsc = np.frombuffer(data, np.float64, rank, off + 8 * rank)
+        off += 16 * rank
+        blocks.append((info["row0"], info["row1"], info["col0"], info["col1"], rank, len(widths), 0, 0))
+        lbase, rbase = sum(len(a) for a in lw), sum(len(a) for a in rw)
+        lo = ro = 0
+        for j in range(rank):
+            loff.append(lbase + lo)
+            roff.append(rbase + ro)
+            lo += (rows * int(w[j]) + 31) // 32
+            ro += (cols * int(w[j]) + 31) // 32
+        lw.append(np.frombuffer(data, np.uint32, lo, off))
+        rw.append(np.frombuffer(data, np.uint32, ro, off + 4 * lo))
+        off += 4 * (lo + ro)
+        widths.extend(w)
+        ls.extend(lsc)
+        rs.extend(rsc)
+    h = HMatrix.from_arrays(m.order, perm, blocks, np.concatenate(dense), np.concatenate(lw),
+                            np.concatenate(rw), loff, roff, ls, rs, widths)
+    ref = HMatrix.from_bytes(data)
+    assert np.array_equal(h.matmul(g["x"]), ref.matmul(g["x"]))
