@@ -1,0 +1,400 @@
+#!/usr/bin/env python3
+"""Benchmark of the resident quantized H-matrix matvec (one JSON line).
+
+Workload (default ``cfg2``): the plain method at scale -- n = 32768 points
+uniform in the unit square (numpy default_rng(1)), kernel
+A_ij = -log(|x_i - x_j| + 1e-3), leaf_size 64, bit widths (4,8,12,16,24,32),
+single FP64 right-hand side drawn from the same generator after the points.
+The requested tolerance 1e-8 is infeasible for this matrix in the reference
+(InfeasibleError at block (0:64, 64:128)); 1e-7 and 3e-7 are infeasible at
+n = 32768 too, so the matrix is built at the tightest feasible tolerance of
+that ladder, 1e-6, and the line states both.  The matrix is constructed on
+this machine by qhmat_gb300.construct (byte-identical to the reference's
+from_dense + save on the same NumPy build); the data are synthetic.
+
+A step is one apply y = A x.  ``value`` is the packed-byte traffic model
+(codes + two FP64 scales per component + dense diagonal + x read + y write)
+divided by the device time per step, with x and y resident in HBM; the
+representation (~200 MB) is larger than the 129 MB L2, so no flush is needed
+between steps.  ``e2e`` is the same metric through the host-buffer C-ABI call
+(qh_matmul_host: pinned H2D copy of x, apply, D2H copy of y, all timed).
+
+``--impl reference`` times the reference's CPU HMatrix::matmul on the host
+cores instead: the reference core compiled from its sources (oracle/_ref)
+where that build loads, else the bit-identical plain-C restatement
+(oracle/qhmat_oracle.c) with every host thread.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WORKLOADS = {
+    "cfg2": dict(n=32768, dim=2, seed=1, kernel="log", leaf=64, tol_requested=1e-8, tol=1e-6, rhs=1,
+                 desc="plain at scale: n=32768 uniform unit square (seed 1), -log(r+1e-3), leaf 64, "
+                      "widths 4/8/12/16/24/32, single RHS"),
+    "cfg1": dict(n=2048, dim=1, seed=0, kernel="inverse", leaf=32, tol_requested=1e-6, tol=1e-6, rhs=4,
+                 desc="plain CPU-runnable: n=2048 linspace, 1/(r+0.4), leaf 32, RHS 2048x4 seed 0"),
+}
+
+
+def make_inputs(name: str, workers: int):
+    import numpy as np
+
+    from qhmat_gb300 import construct
+
+    wl = WORKLOADS[name]
+    if name == "cfg1":
+        pts = np.linspace(0, 1, wl["n"])[:, None]
+        x = np.random.default_rng(0).standard_normal((wl["n"], wl["rhs"]))
+    else:
+        rng = np.random.default_rng(wl["seed"])
+        pts = rng.random((wl["n"], wl["dim"]))
+        x = rng.standard_normal(wl["n"]) if wl["rhs"] == 1 else rng.standard_normal((wl["n"], wl["rhs"]))
+    t0 = time.time()
+    img = construct.from_kernel(pts, wl["kernel"], tolerance=wl["tol"], leaf_size=wl["leaf"],
+                                workers=workers)
+    data = construct.to_qhmat_bytes(img)
+    return data, x, time.time() - t0
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-i", str(self.index), "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in getattr(self, "lines", []):
+            f = [v.strip() for v in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs, burst copy)"
+    return 6800.0, "fallback (6.8 TB/s)"
+
+
+def cpu_baseline(data: bytes, x, model_bytes: int, budget_s: float = 10.0) -> dict:
+    """Reference-arm CPU apply on all host cores over a bounded sample."""
+    from oracle import oracle
+
+    threads = os.cpu_count() or 1
+    kind, impl = "port", None
+    if oracle.reference_available():
+        try:
+            impl = oracle.RefMatrix(data)
+            kind, threads = "reference", 1
+        except OSError:
+            impl = None
+    if impl is None:
+        impl = oracle.OracleMatrix(data)
+
+    def run():
+        return impl.matmul(x) if kind == "reference" else impl.matmul(x, threads=threads)
+
+    y = run()  # warm-up
+    reps, t0 = 0, time.perf_counter()
+    while reps < 3 or (time.perf_counter() - t0 < budget_s and reps < 10000):
+        run()
+        reps += 1
+    dt = time.perf_counter() - t0
+    return {"value": model_bytes * reps / dt / 1e9, "unit": "GB/s", "cores": threads, "kind": kind,
+            "sample": f"{reps} full applies of the bench workload in {dt:.1f} s "
+                      f"({1e3 * dt / reps:.2f} ms each, {threads} thread(s))"}, y
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def run_reference_arm(args):
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return 0
+    import numpy as np
+
+    data, x, build_s = make_inputs(args.workload, os.cpu_count() or 1)
+    from oracle import oracle
+
+    wl = WORKLOADS[args.workload]
+    m = oracle.OracleMatrix(data)
+    import ctypes
+
+    model = _model_bytes(data, x)
+    base, _ = cpu_baseline(data, x, model, budget_s=min(30.0, 5.0 + 0.02 * args.steps))
+    out = {
+        "impl": "reference", "metric": "H-matvec GB/s (% HBM peak)", "value": base["value"], "unit": "GB/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": model / (base["value"] * 1e9) * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (constructed on the host, seeded)",
+        "config": _config(args.workload, wl, build_s),
+        "cpu_baseline": base,
+        "e2e": {"value": base["value"], "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+def _model_bytes(data: bytes, x) -> int:
+    """Packed-byte model from a QHMAT001 image (no device needed)."""
+    from oracle import oracle
+
+    m = oracle.OracleMatrix(data)
+    codes = scales = dense = 0
+    for b in range(m.block_count):
+        info = m.block_info(b)
+        if info["dense"]:
+            dense += 8 * (info["row1"] - info["row0"]) * (info["col1"] - info["col0"])
+        else:
+            codes += 4 * (info["left_words"] + info["right_words"])
+            scales += 16 * info["rank"]
+    rhs = 1 if x.ndim == 1 else x.shape[1]
+    return codes + scales + dense + 16 * m.order * rhs
+
+
+def _config(name, wl, build_s):
+    return {"workload": f"{name}: {wl['desc']}", "n": wl["n"], "rhs": wl["rhs"],
+            "tolerance": wl["tol"], "tolerance_requested": wl["tol_requested"],
+            "tolerance_note": ("requested tolerance infeasible in the reference; tightest feasible of "
+                               "the ladder 1e-8/3e-8/1e-7/3e-7/1e-6") if wl["tol"] != wl["tol_requested"] else "",
+            "l2": "representation larger than L2 (129 MB); no flush between steps",
+            "construction_s": round(build_s, 1)}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="cfg2", choices=sorted(WORKLOADS))
+    ap.add_argument("--e2e-steps", type=int, default=200)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        raise SystemExit("--warmup must be >= 3")
+    if args.impl == "reference":
+        return run_reference_arm(args)
+
+    world, rank, local = dist_setup()
+    import numpy as np
+
+    # Build the matrix (CPU, spawn pool) before the first CUDA call.
+    workers = max(1, (os.cpu_count() or 1) // max(1, world))
+    data, x, build_s = make_inputs(args.workload, workers)
+
+    import torch
+
+    import qhmat_gb300
+    from qhmat_gb300 import _lib
+
+    torch.cuda.set_device(local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        pg = dist
+    lib = _lib.load_library()
+    h = qhmat_gb300.HMatrix.from_bytes(data, device=local)
+    wl = WORKLOADS[args.workload]
+    rhs = wl["rhs"]
+    model = h.model_bytes(rhs)
+    st = h.stats
+
+    dev = torch.device("cuda", local)
+    xd = torch.from_numpy(np.ascontiguousarray(x)).to(dev)
+    yd = torch.empty_like(xd)
+    need = h.workspace_bytes(rhs)
+    ws = torch.empty(need, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    K, W = args.steps, args.warmup
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(K + W)]
+    ev_ptrs = [(torch.cuda.Event * 0)] if False else None
+
+    import ctypes as C
+
+    def step(i):
+        arr = (C.c_void_p * 4)(*[e.cuda_event for e in evs[i]])
+        rc = lib.qh_matmul_device_profiled(h._h, xd.data_ptr(), yd.data_ptr(), rhs, ws.data_ptr(), need,
+                                           stream.cuda_stream, None, arr)
+        if rc:
+            _lib.raise_for(rc)
+
+    # Events must exist on the device before their handles are recorded.
+    for row in evs:
+        for e in row:
+            e.record(stream)
+    torch.cuda.synchronize()
+    for i in range(W):
+        step(i)
+    torch.cuda.synchronize()
+    if pg:
+        pg.barrier()
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        if pg:
+            pg.barrier()
+        t_start.record(stream)
+        wall0 = time.perf_counter()
+        for i in range(W, W + K):
+            step(i)
+        t_end.record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - wall0
+        if pg:
+            pg.barrier()
+    total_ms = t_start.elapsed_time(t_end)
+    if pg:
+        t = torch.tensor([total_ms], device=dev)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_step = total_ms / K
+    # per-kernel durations over the timed steps
+    kern = {"prep_x": [], "column": [], "row": []}
+    for i in range(W, W + K):
+        e = evs[i]
+        kern["prep_x"].append(e[0].elapsed_time(e[1]))
+        kern["column"].append(e[1].elapsed_time(e[2]))
+        kern["row"].append(e[2].elapsed_time(e[3]))
+    kmean = {k: statistics.mean(v) for k, v in kern.items()}
+    # algorithmic bytes per launch of each kernel (packed-byte model split by side)
+    import struct
+
+    # left / right code bytes from the image
+    from oracle import oracle as _o
+
+    om = _o.OracleMatrix(data)
+    lw = rw = 0
+    for b in range(om.block_count):
+        inf = om.block_info(b)
+        if not inf["dense"]:
+            lw += inf["left_words"]
+            rw += inf["right_words"]
+    n = h.order
+    comps = st["components"]
+    alg = {
+        "prep_x": 16 * n * rhs,                                     # x read, fixed-point x written
+        "column": 4 * rw + 8 * comps + 8 * n * rhs,                 # Q codes, s^P s^Q, x once
+        "row": 4 * lw + 8 * comps * rhs + st["dense_bytes"] + 16 * n * rhs,  # P codes, U, diag, x, y
+    }
+    dom = max(kmean, key=lambda k: kmean[k])
+    peak, peak_src = measured_peak()
+    achieved = alg[dom] / (kmean[dom] * 1e-3) / 1e9
+    traffic_file = ROOT / "profiles" / f"traffic_{args.workload}.json"
+    traffic = None
+    if traffic_file.exists():
+        try:
+            traffic = json.loads(traffic_file.read_text()).get(dom)
+        except ValueError:
+            traffic = None
+    value = model * world / (ms_step * 1e-3) / 1e9
+
+    # parity of the timed result against the oracle (same inputs)
+    y_gpu = yd.cpu().numpy()
+    out = {
+        "metric": "H-matvec GB/s (% HBM peak)", "value": round(value, 2), "unit": "GB/s",
+        "n_gpus": world, "steps": K, "warmup": W, "ms_per_step": round(ms_step, 5),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64 (int2..int32 codes x 54-bit fixed-point x; FP64 scales, diagonal, accumulation)",
+        "data": "synthetic (seeded points; matrix constructed on the host)",
+        "config": dict(_config(args.workload, wl, build_s), parallelism=f"replicas x{world}",
+                       model_bytes=model, components=comps, blocks=st["block_count"]),
+        "pct_hbm_peak": round(100 * value / world / peak, 1),
+        "rhs_per_s": round(rhs * world / (ms_step * 1e-3), 1),
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
+                     "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
+                     "peak_source": peak_src, "algorithmic_bytes": alg[dom],
+                     "kernel_ms": {k: round(v, 5) for k, v in kmean.items()},
+                     "whole_apply_frac": round(value / world / peak, 4)},
+        "gpu_launches": 3 * K,
+        "clocks": clk.summary(),
+        "wall_ms_per_step": round(1e3 * wall / K, 5),
+    }
+    if rank == 0:
+        # e2e: host buffers through qh_matmul_host (H2D + apply + D2H timed)
+        xh = np.ascontiguousarray(x)
+        for _ in range(3):
+            h.matmul(xh)
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            y_host = h.matmul(xh)
+        e2e_s = (time.perf_counter() - t0) / args.e2e_steps
+        out["e2e"] = {"value": round(model / e2e_s / 1e9, 2), "unit": "GB/s",
+                      "h2d_bytes_per_step": int(xh.nbytes), "d2h_bytes_per_step": int(y_host.nbytes),
+                      "ms_per_step": round(1e3 * e2e_s, 4)}
+        if not args.no_cpu_baseline:
+            base, y_cpu = cpu_baseline(data, x, model)
+            out["cpu_baseline"] = base
+            err = float(np.linalg.norm(y_gpu - y_cpu) / np.linalg.norm(y_cpu))
+            out["parity"] = {"rel_err_vs_oracle": err, "tolerance": 1e-13,
+                             "host_path_equals_device_path": bool(np.array_equal(y_host, y_gpu))}
+        print(json.dumps(out), flush=True)
+    if pg:
+        pg.barrier()
+        pg.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -120,12 +120,25 @@ QH_API size_t qh_workspace_bytes(const qh_matrix* m, size_t rhs);
 QH_API int qh_matmul_device(const qh_matrix* m, const double* x, double* y, size_t rhs,
                      void* workspace, size_t workspace_bytes, void* stream, int* status);
 
+/* qh_matmul_device that also records four caller-created cudaEvent_t on
+ * `stream`: before the right-hand-side preparation kernel, before the
+ * column-side kernel, before the row-side kernel, and after it.  Profiling
+ * aid (per-kernel durations); the work done is identical. */
+QH_API int qh_matmul_device_profiled(const qh_matrix* m, const double* x, double* y, size_t rhs,
+                                     void* workspace, size_t workspace_bytes, void* stream,
+                                     int* status, void* const* events4);
+
 /* Drop-in for HMatrix::matmul_cuda: host x (order*rhs doubles), host y.
  * Copies x in through pinned staging, applies, copies y back and
  * synchronises.  Raises the reference's errors: "right-hand-side shape
  * mismatch", "nonfinite right-hand side" (QH_EINVAL), "CUDA launch grid too
  * large" (QH_EOVERFLOW), "no CUDA device is available" (QH_ERUNTIME). */
 QH_API int qh_matmul_host(const qh_matrix* m, const double* x, double* y, size_t rhs);
+
+/* FNV-1a-64 of a byte range, the QHMAT001 trailer checksum (offset basis
+ * 14695981039346656037, prime 1099511628211; src/qhmat/io.cpp:18-19, 42).
+ * Used when writing QHMAT001 images. */
+QH_API uint64_t qh_fnv1a64(const void* bytes, size_t len);
 
 /* Validation aid: decode every stored code of one factor side on the device
  * with the same device routine the apply kernels use, and copy the integers

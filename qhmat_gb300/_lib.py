@@ -64,8 +64,12 @@ def load_library() -> C.CDLL:
     lib.qh_workspace_bytes.argtypes = [vp, sz]
     lib.qh_matmul_device.restype = i32
     lib.qh_matmul_device.argtypes = [vp, vp, vp, sz, vp, sz, vp, vp]
+    lib.qh_matmul_device_profiled.restype = i32
+    lib.qh_matmul_device_profiled.argtypes = [vp, vp, vp, sz, vp, sz, vp, vp, vp]
     lib.qh_matmul_host.restype = i32
     lib.qh_matmul_host.argtypes = [vp, vp, vp, sz]
+    lib.qh_fnv1a64.restype = C.c_uint64
+    lib.qh_fnv1a64.argtypes = [C.c_char_p, sz]
     lib.qh_debug_decode.restype = i32
     lib.qh_debug_decode.argtypes = [vp, i32, vp, sz, C.POINTER(sz)]
     _lib = lib

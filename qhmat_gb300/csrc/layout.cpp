@@ -7,6 +7,8 @@
 // the reference's Reader class.
 #include "layout.hpp"
 
+#include "../../include/qhmat_gb300.h"
+
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -17,8 +19,8 @@
 namespace qhg {
 namespace {
 
-constexpr uint64_t kFnvOffset = 14695981039346656037ULL;  // io.cpp:18
-constexpr uint64_t kFnvPrime = 1099511628211ULL;          // io.cpp:19
+constexpr uint64_t kFnvOffset = kFnvOffsetBasis;
+constexpr uint64_t kFnvPrime = kFnvPrimeValue;
 
 // Cursor over the image.  `avail` counts bytes before the 8-byte trailer.
 class Cursor {
@@ -413,3 +415,10 @@ Layout build_layout(const HostMatrix& m) {
 }
 
 }  // namespace qhg
+
+extern "C" uint64_t qh_fnv1a64(const void* bytes, size_t len) {
+    const auto* p = static_cast<const uint8_t*>(bytes);
+    uint64_t h = qhg::kFnvOffsetBasis;
+    for (size_t i = 0; i < len; ++i) h = (h ^ p[i]) * qhg::kFnvPrimeValue;
+    return h;
+}

@@ -93,6 +93,10 @@ struct Layout {
 
 Layout build_layout(const HostMatrix& m);
 
+// QHMAT001 trailer: FNV-1a-64 (src/qhmat/io.cpp:18-19).
+constexpr uint64_t kFnvOffsetBasis = 14695981039346656037ULL;
+constexpr uint64_t kFnvPrimeValue = 1099511628211ULL;
+
 // Rows of one row tile at most (one CTA of the row-side kernel).
 constexpr int kTileRows = 64;
 // x entries per exponent chunk of the fixed-point right-hand side.

@@ -381,6 +381,7 @@ using namespace qhg;
 struct qh_matrix {
     Layout L;
     int device = 0;
+    int sms = 1;
     void* arena = nullptr;  // device copy of L.arena
     Arena A{};
     // lazily allocated scratch for calls without a workspace, and host staging
@@ -446,6 +447,7 @@ int upload(Layout&& L, int device, qh_matrix** out) {
         delete m;
         return cuda_fail(e, "cudaMemcpy host-to-device");
     }
+    cudaDeviceGetAttribute(&m->sms, cudaDevAttrMultiProcessorCount, device);
     // The host image is no longer needed once uploaded.
     std::vector<uint8_t>().swap(m->L.arena);
     const Sections& S = m->L.sec;
@@ -506,7 +508,7 @@ WsPlan ws_plan(const Layout& L, size_t rhs) {
 size_t ws_bytes(const Layout& L, size_t rhs) { return ws_plan(L, rhs).total; }
 
 int launch(const qh_matrix* m, const double* x, double* y, size_t rhs, void* ws, cudaStream_t s,
-           int* status) {
+           int* status, void* const* ev = nullptr) {
     const Layout& L = m->L;
     const int n = int(L.order);
     auto* w = static_cast<uint8_t*>(ws);
@@ -517,15 +519,20 @@ int launch(const qh_matrix* m, const double* x, double* y, size_t rhs, void* ws,
     W.u = reinterpret_cast<double*>(w + P.u);
     W.U = reinterpret_cast<int2*>(w + P.U);
     W.ub = reinterpret_cast<int*>(w + P.ub);
+    auto mark = [&](int i) {
+        if (ev) cudaEventRecord(static_cast<cudaEvent_t>(ev[i]), s);
+    };
     const long long prep_warps = (long long)L.n_chunks * (long long)rhs;
+    mark(0);
     prep_x_kernel<<<unsigned((prep_warps + 7) / 8), 256, 0, s>>>(m->A, W, x, n, int(rhs), L.n_chunks, status);
+    mark(1);
     if (L.n_a > 0) {
-        int sms = 0;
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, m->device);
-        const int grid = std::max(1, std::min((L.n_a + 7) / 8, sms * 8));
+        const int grid = std::max(1, std::min((L.n_a + 7) / 8, m->sms * 8));
         column_kernel<<<grid, 256, 0, s>>>(m->A, W, L.n_a, n, int(rhs), L.n_chunks, L.n_comp, L.n_lr);
     }
+    mark(2);
     row_kernel<<<L.n_tiles, kTileRows, 0, s>>>(m->A, W, x, y, n, int(rhs), L.n_comp, L.n_lr);
+    mark(3);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "CUDA kernel launch");
     return QH_OK;
@@ -644,6 +651,11 @@ size_t qh_workspace_bytes(const qh_matrix* m, size_t rhs) { return m ? ws_bytes(
 
 int qh_matmul_device(const qh_matrix* m, const double* x, double* y, size_t rhs, void* workspace,
                      size_t workspace_bytes, void* stream, int* status) {
+    return qh_matmul_device_profiled(m, x, y, rhs, workspace, workspace_bytes, stream, status, nullptr);
+}
+
+int qh_matmul_device_profiled(const qh_matrix* m, const double* x, double* y, size_t rhs, void* workspace,
+                              size_t workspace_bytes, void* stream, int* status, void* const* events4) {
     if (!m) return fail(QH_EINVAL, "null matrix handle");
     int rc = check_rhs(m, rhs);
     if (rc) return rc;
@@ -653,7 +665,7 @@ int qh_matmul_device(const qh_matrix* m, const double* x, double* y, size_t rhs,
     if (workspace) {
         if (workspace_bytes < need) return fail(QH_EINVAL, "workspace too small");
         if (reinterpret_cast<uintptr_t>(workspace) & 255) return fail(QH_EINVAL, "workspace must be 256-byte aligned");
-        return launch(m, x, y, rhs, workspace, static_cast<cudaStream_t>(stream), status);
+        return launch(m, x, y, rhs, workspace, static_cast<cudaStream_t>(stream), status, events4);
     }
     auto* mm = const_cast<qh_matrix*>(m);
     std::lock_guard<std::mutex> lock(mm->mu);
@@ -665,7 +677,7 @@ int qh_matmul_device(const qh_matrix* m, const double* x, double* y, size_t rhs,
         if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc");
         mm->own_ws_bytes = need;
     }
-    return launch(m, x, y, rhs, mm->own_ws, static_cast<cudaStream_t>(stream), status);
+    return launch(m, x, y, rhs, mm->own_ws, static_cast<cudaStream_t>(stream), status, events4);
 }
 
 int qh_matmul_host(const qh_matrix* m, const double* x, double* y, size_t rhs) {
