@@ -268,6 +268,24 @@ T* at(std::vector<uint8_t>& arena, size_t off) {
     return reinterpret_cast<T*>(arena.data() + off);
 }
 
+// Copy the bit string [bit0, bit0 + nbits) of a run of `run_words` words to
+// out[0 .. ceil(nbits/32)), starting at a fresh word; bits past the string
+// (or past the run) are zero.
+void copy_bits(const uint32_t* run, uint64_t run_words, uint64_t bit0, uint64_t nbits, uint32_t* out) {
+    const uint64_t nw = (nbits + 31) / 32;
+    for (uint64_t i = 0; i < nw; ++i) {
+        const uint64_t b = bit0 + 32 * i;
+        const uint64_t wi = b >> 5;
+        const unsigned sh = unsigned(b & 31);
+        const uint64_t lo = wi < run_words ? run[wi] : 0;
+        const uint64_t hi = wi + 1 < run_words ? run[wi + 1] : 0;
+        uint32_t v = uint32_t(((hi << 32) | lo) >> sh);
+        const uint64_t rem = nbits - 32 * i;
+        if (rem < 32) v &= (1u << rem) - 1u;
+        out[i] = v;
+    }
+}
+
 }  // namespace
 
 Layout build_layout(const HostMatrix& m) {
@@ -276,49 +294,117 @@ Layout build_layout(const HostMatrix& m) {
     L.bound = m.reconstruction_bound();
     if (m.order >= (1ull << 31)) throw overflow_error("matrix order too large for the device layout");
     if (m.width.size() >= (1ull << 31)) throw overflow_error("too many components for the device layout");
-    if (m.left_words.size() >= (1ull << 32) || m.right_words.size() >= (1ull << 32))
-        throw overflow_error("packed factors too large for the device layout");
 
     std::vector<LowRankDesc> lr;
     std::vector<DenseDesc> dd;
-    std::vector<int32_t> block_item(m.blocks.size());  // item code per block
+    std::vector<int32_t> block_item(m.blocks.size());
+    std::vector<size_t> block_of_lr;
+    std::vector<double> dense_cm;  // column-major copies
     for (size_t k = 0; k < m.blocks.size(); ++k) {
         const auto& b = m.blocks[k];
         const int32_t r0 = int32_t(b.row0), mm = int32_t(b.row1 - b.row0);
         const int32_t c0 = int32_t(b.col0), nn = int32_t(b.col1 - b.col0);
         if (b.dense) {
             block_item[k] = -1 - int32_t(dd.size());
-            dd.push_back({r0, mm, c0, nn, int64_t(b.dense_off)});
+            dd.push_back({r0, mm, c0, nn, int64_t(dense_cm.size())});
+            const double* src = m.dense.data() + b.dense_off;
+            const size_t base = dense_cm.size();
+            dense_cm.resize(base + size_t(mm) * size_t(nn));
+            for (int32_t i = 0; i < mm; ++i)
+                for (int32_t c = 0; c < nn; ++c) dense_cm[base + size_t(c) * mm + i] = src[size_t(i) * nn + c];
             L.dense_bytes += 8ull * uint64_t(mm) * uint64_t(nn);
             L.flops += 2ull * uint64_t(mm) * uint64_t(nn);
         } else {
             block_item[k] = int32_t(lr.size());
             lr.push_back({r0, mm, c0, nn, int32_t(b.rank), int32_t(b.comp0)});
+            block_of_lr.push_back(k);
             L.scale_bytes += 16ull * b.rank;
             L.flops += 2ull * b.rank * uint64_t(mm + nn);
             for (uint64_t j = 0; j < b.rank; ++j) {
                 const int w = m.width[b.comp0 + j];
-                L.code_bytes += 4ull * (words_for(uint64_t(mm), w) + words_for(uint64_t(nn), w));
+                L.left_code_bytes += 4ull * words_for_bits(uint64_t(mm), w);
+                L.right_code_bytes += 4ull * words_for_bits(uint64_t(nn), w);
             }
         }
     }
+    L.code_bytes = L.left_code_bytes + L.right_code_bytes;
     L.n_lr = int32_t(lr.size());
     L.n_dense = int32_t(dd.size());
     L.n_comp = int32_t(m.width.size());
     L.n_chunks = int32_t((m.order + kChunk - 1) / kChunk);
 
-    // Column side: low-rank blocks with rank > 0, heaviest first.
-    std::vector<int32_t> a_order;
-    for (int32_t i = 0; i < L.n_lr; ++i)
-        if (lr[i].rank > 0) a_order.push_back(i);
-    std::stable_sort(a_order.begin(), a_order.end(), [&](int32_t a, int32_t b) {
-        return int64_t(lr[a].rank) * lr[a].n > int64_t(lr[b].rank) * lr[b].n;
+    // ---- column side: tasks of <= 32 components sharing (col0, n, width).
+    struct Key {
+        int32_t col0, n, w;
+        bool operator<(const Key& o) const {
+            if (col0 != o.col0) return col0 < o.col0;
+            if (n != o.n) return n < o.n;
+            return w < o.w;
+        }
+    };
+    std::vector<std::pair<Key, int32_t>> comps;  // (key, component id), in block order
+    for (const auto& d : lr)
+        for (int32_t j = 0; j < d.rank; ++j)
+            comps.push_back({{d.col0, d.n, int32_t(m.width[d.comp0 + j])}, d.comp0 + j});
+    std::stable_sort(comps.begin(), comps.end(),
+                     [](const auto& a, const auto& b) { return a.first < b.first; });
+    std::vector<ColTask> tasks;
+    std::vector<int32_t> task_comp;
+    std::vector<uint32_t> qwords;
+    int32_t n_split = 0;
+    for (size_t i = 0; i < comps.size();) {
+        size_t j = i;
+        while (j < comps.size() && !(comps[i].first < comps[j].first) && !(comps[j].first < comps[i].first)) ++j;
+        for (size_t t0 = i; t0 < j; t0 += 32) {
+            const int32_t count = int32_t(std::min<size_t>(32, j - t0));
+            const Key key = comps[t0].first;
+            const int32_t nchunks = (key.n + kColChunk - 1) / kColChunk;
+            const int32_t stride = (count * key.w + 3) / 4 * 4;
+            const int32_t comp_idx = int32_t(task_comp.size());
+            for (int32_t l = 0; l < count; ++l) task_comp.push_back(comps[t0 + l].second);
+            const size_t base = qwords.size();  // multiple of 4 words
+            qwords.resize(base + size_t(nchunks) * stride, 0);
+            for (int32_t l = 0; l < count; ++l) {
+                const int32_t c = comps[t0 + l].second;
+                const uint32_t* run = m.right_words.data() + m.right_off[c];
+                const uint64_t run_words = words_for_bits(uint64_t(key.n), key.w);
+                for (int32_t ch = 0; ch < nchunks; ++ch)
+                    for (int32_t v = 0; v < key.w; ++v) {
+                        const uint64_t wi = uint64_t(ch) * key.w + v;
+                        qwords[base + size_t(ch) * stride + size_t(v) * count + l] = wi < run_words ? run[wi] : 0u;
+                    }
+            }
+            const int32_t nparts = (nchunks + kMaxPartChunks - 1) / kMaxPartChunks;
+            const int32_t split_id = nparts > 1 ? n_split++ : -1;
+            L.max_parts = std::max(L.max_parts, nparts);
+            for (int32_t pt = 0; pt < nparts; ++pt) {
+                ColTask T{};
+                T.col0 = key.col0;
+                T.n = key.n;
+                T.width = key.w;
+                T.count = count;
+                T.word0 = int64_t(base);
+                T.stride = stride;
+                T.comp_idx = comp_idx;
+                T.chunk0 = pt * kMaxPartChunks;
+                T.nchunks = std::min(kMaxPartChunks, nchunks - T.chunk0);
+                T.part = pt;
+                T.nparts = nparts;
+                T.split_id = split_id;
+                tasks.push_back(T);
+            }
+        }
+        i = j;
+    }
+    // heaviest units first
+    std::stable_sort(tasks.begin(), tasks.end(), [](const ColTask& a, const ColTask& b) {
+        return int64_t(a.nchunks) * a.width * a.count > int64_t(b.nchunks) * b.width * b.count;
     });
-    L.n_a = int32_t(a_order.size());
+    L.n_tasks = int32_t(tasks.size());
+    L.n_split = n_split;
+    L.stored_q_words = qwords.size();
 
-    // Row side: elementary slabs (finalize's row boundaries), each cut into
-    // tiles of at most kTileRows rows.  A slab's items are the blocks covering
-    // it, in insertion order.
+    // ---- row side: elementary slabs (finalize's row boundaries) cut into tiles.
     std::vector<uint64_t> bounds{0, m.order};
     for (const auto& b : m.blocks) {
         bounds.push_back(b.row0);
@@ -327,33 +413,73 @@ Layout build_layout(const HostMatrix& m) {
     std::sort(bounds.begin(), bounds.end());
     bounds.erase(std::unique(bounds.begin(), bounds.end()), bounds.end());
     const size_t n_slabs = bounds.size() - 1;
-    std::vector<std::vector<int32_t>> slab_items(n_slabs);
+    std::vector<std::vector<int32_t>> slab_blocks(n_slabs);
     for (size_t k = 0; k < m.blocks.size(); ++k) {
         const auto& b = m.blocks[k];
         size_t s = size_t(std::lower_bound(bounds.begin(), bounds.end(), b.row0) - bounds.begin());
-        for (; s < n_slabs && bounds[s] < b.row1; ++s) slab_items[s].push_back(block_item[k]);
+        for (; s < n_slabs && bounds[s] < b.row1; ++s) slab_blocks[s].push_back(int32_t(k));
     }
-    std::vector<int32_t> items;
+    std::vector<RowItem> items;
     std::vector<RowTile> tiles;
     std::vector<int64_t> tile_work;
+    std::vector<uint32_t> pwords;
+    const uint64_t max_block_words = kStageWordBytes / 4;
     for (size_t s = 0; s < n_slabs; ++s) {
-        const int32_t i0 = int32_t(items.size());
-        int64_t comp_sum = 0, work_per_row = 0;
-        for (int32_t it : slab_items[s]) {
-            items.push_back(it);
-            if (it >= 0) {
-                comp_sum += lr[it].rank;
-                work_per_row += lr[it].rank;
-            } else {
-                work_per_row += dd[-1 - it].n;
-            }
-        }
-        const int32_t i1 = int32_t(items.size());
-        L.max_tile_items_comp = std::max<int32_t>(L.max_tile_items_comp, int32_t(comp_sum));
         for (uint64_t r = bounds[s]; r < bounds[s + 1]; r += kTileRows) {
             const int32_t rows = int32_t(std::min<uint64_t>(kTileRows, bounds[s + 1] - r));
-            tiles.push_back({int32_t(r), rows, i0, i1});
-            tile_work.push_back(work_per_row * rows);
+            RowTile T{int32_t(r), rows, int32_t(items.size()), 0};
+            int64_t work = 0;
+            for (int32_t k : slab_blocks[s]) {
+                const auto& b = m.blocks[size_t(k)];
+                const int32_t rloc0 = int32_t(r - b.row0);
+                if (b.dense) {
+                    RowItem it{};
+                    it.block = block_item[size_t(k)];
+                    it.rloc0 = rloc0;
+                    const DenseDesc& d = dd[size_t(-1 - it.block)];
+                    it.off = d.off + rloc0;
+                    items.push_back(it);
+                    work += int64_t(rows) * d.n * 4;
+                    continue;
+                }
+                const uint64_t rows_b = b.row1 - b.row0;
+                for (uint64_t j0 = 0; j0 < b.rank;) {
+                    // greedy group: <= 32 components whose pieces fit one stage
+                    uint64_t j1 = j0, words = kRowHeaderWords;
+                    while (j1 < b.rank && j1 - j0 < 32) {
+                        const uint64_t pw = words_for_bits(uint64_t(rows), m.width[b.comp0 + j1]);
+                        if (words + pw > max_block_words) break;
+                        words += pw;
+                        ++j1;
+                    }
+                    RowItem it{};
+                    it.block = block_item[size_t(k)];
+                    it.rloc0 = rloc0;
+                    it.comp = int32_t(b.comp0 + j0);
+                    it.count = int32_t(j1 - j0);
+                    it.off = int64_t(pwords.size());
+                    const uint64_t total = (words + 3) / 4 * 4;
+                    it.words = int32_t(total);
+                    const size_t base = pwords.size();
+                    pwords.resize(base + total, 0);
+                    auto* hdr = reinterpret_cast<uint8_t*>(pwords.data() + base);
+                    size_t o = base + kRowHeaderWords;
+                    for (uint64_t j = j0; j < j1; ++j) {
+                        const uint64_t c = b.comp0 + j;
+                        const int w = m.width[c];
+                        hdr[j - j0] = uint8_t(w);
+                        copy_bits(m.left_words.data() + m.left_off[c], words_for_bits(rows_b, w),
+                                  uint64_t(rloc0) * w, uint64_t(rows) * w, pwords.data() + o);
+                        o += words_for_bits(uint64_t(rows), w);
+                    }
+                    items.push_back(it);
+                    work += int64_t(rows) * int64_t(j1 - j0) + 64;
+                    j0 = j1;
+                }
+            }
+            T.item1 = int32_t(items.size());
+            tiles.push_back(T);
+            tile_work.push_back(work);
         }
     }
     std::vector<int32_t> torder(tiles.size());
@@ -364,8 +490,11 @@ Layout build_layout(const HostMatrix& m) {
     for (size_t i = 0; i < tiles.size(); ++i) tiles_sorted[i] = tiles[torder[i]];
     L.n_tiles = int32_t(tiles.size());
     L.n_items = int32_t(items.size());
+    L.stored_p_words = pwords.size();
+    if (qwords.size() >= (1ull << 40) || pwords.size() >= (1ull << 40))
+        throw overflow_error("packed factors too large for the device layout");
 
-    // Arena sections, each 256-byte aligned.
+    // ---- arena sections, each 256-byte aligned.
     Sections& S = L.sec;
     size_t off = 0;
     auto place = [&](size_t bytes) {
@@ -379,14 +508,13 @@ Layout build_layout(const HostMatrix& m) {
     S.dd = place(sizeof(DenseDesc) * dd.size());
     S.comp_w = place(C);
     S.comp_s = place(8 * C);
-    S.comp_qoff = place(4 * C);
-    S.comp_poff = place(4 * C);
-    S.qwords = place(4 * m.right_words.size() + 16);
-    S.pwords = place(4 * m.left_words.size() + 16);
-    S.dense = place(8 * m.dense.size());
-    S.a_order = place(4 * a_order.size());
+    S.tasks = place(sizeof(ColTask) * tasks.size());
+    S.task_comp = place(4 * task_comp.size());
+    S.qwords = place(4 * qwords.size() + 16);
+    S.pwords = place(4 * pwords.size() + 16);
+    S.dense = place(8 * dense_cm.size());
     S.tiles = place(sizeof(RowTile) * tiles.size());
-    S.items = place(4 * items.size());
+    S.items = place(sizeof(RowItem) * items.size());
     S.total = off;
 
     L.arena.assign(S.total, 0);
@@ -399,18 +527,15 @@ Layout build_layout(const HostMatrix& m) {
         // One rounding: s_P * s_Q.  In exact arithmetic the block contribution
         // sum_j (s_P c_P)(sum_k s_Q c_Q x) equals sum_j c_P (s_P s_Q) sum_k c_Q x.
         at<double>(A, S.comp_s)[c] = m.left_scale[c] * m.right_scale[c];
-        at<uint32_t>(A, S.comp_qoff)[c] = uint32_t(m.right_off[c]);
-        at<uint32_t>(A, S.comp_poff)[c] = uint32_t(m.left_off[c]);
     }
-    if (!m.right_words.empty())
-        std::memcpy(A.data() + S.qwords, m.right_words.data(), 4 * m.right_words.size());
-    if (!m.left_words.empty())
-        std::memcpy(A.data() + S.pwords, m.left_words.data(), 4 * m.left_words.size());
-    if (!m.dense.empty()) std::memcpy(A.data() + S.dense, m.dense.data(), 8 * m.dense.size());
-    if (!a_order.empty()) std::memcpy(A.data() + S.a_order, a_order.data(), 4 * a_order.size());
+    if (!tasks.empty()) std::memcpy(at<ColTask>(A, S.tasks), tasks.data(), sizeof(ColTask) * tasks.size());
+    if (!task_comp.empty()) std::memcpy(A.data() + S.task_comp, task_comp.data(), 4 * task_comp.size());
+    if (!qwords.empty()) std::memcpy(A.data() + S.qwords, qwords.data(), 4 * qwords.size());
+    if (!pwords.empty()) std::memcpy(A.data() + S.pwords, pwords.data(), 4 * pwords.size());
+    if (!dense_cm.empty()) std::memcpy(A.data() + S.dense, dense_cm.data(), 8 * dense_cm.size());
     if (!tiles_sorted.empty())
         std::memcpy(A.data() + S.tiles, tiles_sorted.data(), sizeof(RowTile) * tiles_sorted.size());
-    if (!items.empty()) std::memcpy(A.data() + S.items, items.data(), 4 * items.size());
+    if (!items.empty()) std::memcpy(A.data() + S.items, items.data(), sizeof(RowItem) * items.size());
     return L;
 }
 

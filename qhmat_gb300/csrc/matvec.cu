@@ -4,7 +4,8 @@
 // whose balanced factors P (rows) and Q (columns) are stored as per-component
 // signed integer codes of width w_j in [2, 32], bit-packed LSB-first exactly
 // as the reference packs them (src/qhmat/core.cpp:235-267), with one FP64
-// scale per factor and component.
+// scale per factor and component.  The words are permuted for coalesced
+// access (layout.hpp); each code keeps its reference bits.
 //
 // FP64 throughput on GB300 is a small fraction of its integer throughput, so
 // the per-code arithmetic is exact integer arithmetic and FP64 is used only
@@ -12,25 +13,27 @@
 //
 //   prep_x    x (source order) -> clustered order, fixed point: each chunk of
 //             32 clustered entries gets one exponent e and entries
-//             X = round(x * 2^(54-e)), |X| <= 2^54.
-//   column    t_bj = sum_k cQ_kj X_k, exact in integers (codes times the two
-//   side      27-bit limbs of X, int64 accumulation, carry-normalised into a
-//             two-word (H, L) integer), then one conversion per component:
-//             u_bj = (s^P_bj s^Q_bj) * t_bj * 2^(...)  (FP64).
-//             The block's u_bj are then put in fixed point on the block's own
-//             exponent (its largest |u_bj|): U_bj, two 27-bit limbs.
-//   row side  per tile of <= 64 rows of one elementary row slab: for every
-//             block covering the slab, sum_j cP_ij U_bj exactly in integers,
-//             shifted onto the tile's exponent with 16 guard bits into a
-//             128-bit accumulator; dense diagonal rows in FP64; one conversion
-//             per row; one writer per y entry (deterministic, no atomics).
+//             X = round(x * 2^(54-e)), |X| <= 2^54 (plus an FP64 clustered
+//             copy for the dense diagonal blocks).
+//   column    one warp per task of <= 32 components sharing a column range
+//   side      and a width, one component per lane: t = sum_k cQ_k X_k exactly
+//             (codes times the two 27-bit limbs of X, int64 accumulation
+//             folded into a two-word integer every 32 entries), then
+//             u = (s^P s^Q) * t in FP64, one conversion per component.
+//   row side  one CTA per tile of <= 64 rows of one elementary row slab, its
+//             eight warps splitting the blocks covering the tile; two rows per
+//             lane.  A block's u are put in fixed point on the block's own
+//             exponent (U, two 27-bit limbs), sum_j cP_ij U_j is exact, and
+//             the block sum is shifted onto the tile's exponent (16 guard
+//             bits) into a 128-bit accumulator; dense diagonal rows in FP64;
+//             warps combine in shared memory in a fixed order; one writer per
+//             y entry (deterministic, no atomics).
 //
 // The only rounding steps are the fixed-point conversions of x (2^-55 relative
 // to the block's largest |x|) and u (2^-55 relative to the block's largest
 // |u|), the product s^P s^Q, the alignment of blocks more than 2^16 below the
-// tile's largest, and the final
-// FP64 conversions: the result agrees with the reference's FP64 matmul
-// (src/qhmat/core.cpp:360-390) to ~1e-15 relative in norm.
+// tile's largest, and the final FP64 conversions: the result agrees with the
+// reference's FP64 matmul (src/qhmat/core.cpp:360-390) to ~1e-15 in norm.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -48,14 +51,18 @@
 namespace qhg {
 namespace {
 
-// Fixed point: |X|, |U| <= 2^kFixBits, split into two kLimb-bit limbs
-// (low limb unsigned, high limb signed).  A code (|c| < 2^31) times a limb is
-// < 2^58, so an int64 accumulator takes kFoldEvery products before it must be
-// folded into the two-word (H, L) integer.
+// Fixed point: |X|, |U| <= 2^kFixBits, split into two kLimb-bit limbs (low
+// limb unsigned, high limb signed).  A code (|c| < 2^31) times a limb is
+// < 2^58, so an int64 accumulator takes kFoldEvery products before it is
+// folded into a wider integer.
 constexpr int kFixBits = 54;
 constexpr int kLimb = 27;
 constexpr long long kLimbMask = (1LL << kLimb) - 1;
-constexpr int kFoldEvery = 32;
+// (kFoldEvery = kColChunk: one column chunk, or 32 row-side components.)
+// Guard bits of the row accumulator: a block whose largest |u| is within
+// 2^kGuard of the tile's largest is added without rounding.
+constexpr int kGuard = 16;
+
 
 // ---------------------------------------------------------------- helpers
 
@@ -72,7 +79,6 @@ __device__ __forceinline__ long long to_fixed(double v, int emax) {
     const int e = int((bits >> 52) & 0x7FF);
     if (e == 0) return 0;
     const long long mant = (bits & 0xFFFFFFFFFFFFFLL) | 0x10000000000000LL;
-    // v = mant * 2^(e-1075);  scaled = mant * 2^(e - 1075 + kFixBits - emax + 1022)
     const int rs = emax - e + (1075 - 1022 - kFixBits);  // right shift, >= 53 - kFixBits
     long long q;
     if (rs <= 0) q = mant << (-rs);
@@ -80,27 +86,31 @@ __device__ __forceinline__ long long to_fixed(double v, int emax) {
     return bits < 0 ? -q : q;
 }
 
-// Code of entry `row` of a component run starting at word `off`, width w:
-// LSB-first bit field at position row*w, sign-extended (the inverse of
-// HMatrix::pack, as HMatrix::decode reads it: core.cpp:269-282).
-__device__ __forceinline__ int extract_code(const uint32_t* __restrict__ words, uint32_t off,
-                                            int row, int w) {
-    const uint32_t pos = uint32_t(row) * uint32_t(w);
-    const uint32_t wi = off + (pos >> 5);
-    const uint32_t lo = __ldg(words + wi);
-    const uint32_t hi = __ldg(words + wi + 1);
-    const uint32_t raw = __funnelshift_r(lo, hi, pos & 31);
-    return int(raw << (32 - w)) >> (32 - w);
+// Sign-extend the low W bits of r.
+template <int W>
+__device__ __forceinline__ int sext(uint32_t r) {
+    return int(r << (32 - W)) >> (32 - W);
 }
 
-// (hi * 2^kLimb + lo) added into the two-word integer H * 2^32 + L.
-__device__ __forceinline__ void fold(long long hi, long long lo, long long& H, long long& L) {
-    H += (hi >> (32 - kLimb)) + (lo >> 32);
-    L += ((hi & ((1LL << (32 - kLimb)) - 1)) << kLimb) + (lo & 0xFFFFFFFFLL);
+// Code e of a bit string held in registers w[0..]: bits [e*W, e*W + W),
+// LSB-first -- the field HMatrix::decode reads (core.cpp:269-282).  Called
+// from fully unrolled loops, so the word index and shift are constants.
+template <int W>
+__device__ __forceinline__ int code_at(const uint32_t* w, int e) {
+    const int pos = e * W, wi = pos >> 5, off = pos & 31;
+    if (off + W <= 32) return sext<W>(w[wi] >> off);
+    return sext<W>(__funnelshift_r(w[wi], w[wi + 1], off));
 }
 
-__device__ __forceinline__ double two_word_to_double(long long H, long long L) {
-    return fma(double(H), 4294967296.0, double(L));
+// (hi * 2^kLimb + lo) as a 128-bit integer.
+__device__ __forceinline__ __int128 widen(long long hi, long long lo) {
+    return ((__int128)hi << kLimb) + lo;
+}
+
+__device__ __forceinline__ double i128_to_double(__int128 v) {
+    const long long hi = (long long)(v >> 64);
+    const unsigned long long lo = (unsigned long long)v;
+    return fma(double(hi), 18446744073709551616.0, double(lo));
 }
 
 struct Arena {
@@ -109,31 +119,106 @@ struct Arena {
     const DenseDesc* dd;
     const uint8_t* comp_w;
     const double* comp_s;
-    const uint32_t* comp_qoff;
-    const uint32_t* comp_poff;
+    const ColTask* tasks;
+    const int32_t* task_comp;
     const uint32_t* qwords;
     const uint32_t* pwords;
     const double* dense;
-    const int32_t* a_order;
     const RowTile* tiles;
-    const int32_t* items;
+    const RowItem* items;
 };
 
 struct Work {
-    long long* X;   // [rhs][n]        fixed-point x, clustered order
-    int* xexp;      // [rhs][n_chunks] exponent field of each 32-entry chunk
-    double* u;      // [rhs][n_comp]   u_bj = s^P s^Q t_bj (FP64)
-    int2* U;        // [rhs][n_comp]   u_bj in fixed point on its block's exponent, two limbs
-    int* ub;        // [rhs][n_lr]     exponent field of each block's largest |u_bj|
+    double* xc;        // [rhs][n]  x in clustered order (FP64)
+    int* xe;           // [rhs]     largest exponent field of x (zeroed before prep_x)
+    int* split_cnt;    // [n_split][rhs] finished parts of each split column task (zeroed)
+    long long* part;   // [n_split][max_parts][rhs][32][2] partial sums of split tasks
+    double* u;         // [rhs][n_comp] u_bj = s^P s^Q t_bj (FP64)
 };
 
-// Guard bits of the row accumulator: a block whose largest |u| is within
-// 2^kGuard of the tile's largest is added without rounding.
-constexpr int kGuard = 16;
+// ------------------------------------------------------------ cp.async
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    const unsigned s = unsigned(__cvta_generic_to_shared(smem));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+    const unsigned s = unsigned(__cvta_generic_to_shared(smem));
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// One stage of a warp's prefetch pipeline: code words plus 32 doubles (x
+// entries on the column side, u values on the row side).
+struct Stage {
+    uint32_t words[kStageWordBytes / 4];
+    double v[32];
+};
+constexpr int kStages = 3;
+constexpr int kWarps = 8;
+constexpr int kPipeSmem = kWarps * kStages * int(sizeof(Stage));
+
+// ------------------------------------------------------------- decoders
+
+// Column side: the 32 codes of lane `lane`'s chunk `ch` of a task (layout.hpp:
+// word v of the chunk at q[(ch*W + v)*count + lane]).
+template <int W>
+__device__ __forceinline__ void col_chunk_words(const uint32_t* __restrict__ q, int ch, int count, int lane,
+                                                uint32_t (&w)[W]) {
+    const uint32_t* base = q + (size_t)ch * W * count + lane;
+#pragma unroll
+    for (int v = 0; v < W; ++v) w[v] = __ldg(base + (size_t)v * count);
+}
+
+template <int W>
+__device__ __forceinline__ void col_chunk_codes(const uint32_t (&w)[W], int (&c)[32]) {
+#pragma unroll
+    for (int e = 0; e < 32; ++e) c[e] = code_at<W>(w, e);
+}
+
+// Row side: codes of rows 2*lane and 2*lane+1 of a piece (bit string of the
+// tile's rows of one component, starting at a fresh word).  `piece` may point
+// to shared or global memory.
+template <int W>
+__device__ __forceinline__ void row_pair_codes(const uint32_t* piece, int lane, int& c0, int& c1) {
+    const uint32_t pos = uint32_t(lane) * (2 * W);
+    const uint32_t wi = pos >> 5, off = pos & 31;
+    if constexpr (32 % (2 * W) == 0) {
+        // both fields inside one word
+        const uint32_t r = piece[wi] >> off;
+        c0 = sext<W>(r);
+        c1 = sext<W>(r >> W);
+    } else if constexpr (W == 32) {
+        c0 = int(piece[wi]);
+        c1 = int(piece[wi + 1]);
+    } else if constexpr (W <= 16) {
+        const uint32_t lo = piece[wi], hi = piece[wi + 1];
+        const unsigned long long r = (((unsigned long long)hi << 32) | lo) >> off;
+        c0 = sext<W>(uint32_t(r));
+        c1 = sext<W>(uint32_t(r >> W));
+    } else {
+        const uint32_t a = piece[wi], b = piece[wi + 1], d = piece[wi + 2];
+        c0 = sext<W>(__funnelshift_r(a, b, off));
+        // row 2*lane+1 starts at off + W (< 64)
+        const uint32_t p1 = off + W;
+        const uint32_t x0 = p1 < 32 ? a : b, x1 = p1 < 32 ? b : d;
+        c1 = sext<W>(__funnelshift_r(x0, x1, p1 & 31));
+    }
+}
+
+// Dispatch a width to a template instance.
+#define QH_WIDTH_CASES(X) \
+    X(2) X(3) X(4) X(5) X(6) X(7) X(8) X(9) X(10) X(11) X(12) X(13) X(14) X(15) X(16) X(17) \
+    X(18) X(19) X(20) X(21) X(22) X(23) X(24) X(25) X(26) X(27) X(28) X(29) X(30) X(31) X(32)
 
 // ---------------------------------------------------------------- kernels
 
-// One warp per (chunk of 32 clustered positions, rhs column).
+// One warp per (chunk of 32 clustered positions, rhs column): clustered FP64
+// copy of x, largest exponent field per column (atomicMax), nonfinite flag.
 __global__ void __launch_bounds__(256) prep_x_kernel(Arena A, Work W, const double* __restrict__ x,
                                                      int n, int rhs, int n_chunks, int* status) {
     const int lane = threadIdx.x & 31;
@@ -147,213 +232,484 @@ __global__ void __launch_bounds__(256) prep_x_kernel(Arena A, Work W, const doub
     const int e = exp_field(v);
     if (__any_sync(0xFFFFFFFFu, e == 0x7FF) && lane == 0 && status) *status = 1;
     const int emax = __reduce_max_sync(0xFFFFFFFFu, e == 0x7FF ? 0 : e);
-    if (valid) W.X[(long long)p * n + pos] = (e == 0x7FF || emax == 0) ? 0 : to_fixed(v, emax);
-    if (lane == 0) W.xexp[p * n_chunks + chunk] = emax;
+    if (valid) W.xc[(long long)p * n + pos] = e == 0x7FF ? 0.0 : v;
+    if (lane == 0 && emax) atomicMax(W.xe + p, emax);
 }
 
-// Column side: one warp per low-rank block at a time (persistent warps over
-// the blocks, heaviest first).  Lanes own entries k = lane + 32 e; components
-// are processed eight at a time and reduced across the warp with a transposed
-// multi-reduction (lane l ends up holding component l >> 2).
-__global__ void __launch_bounds__(256) column_kernel(Arena A, Work W, int n_a, int n, int rhs,
-                                                     int n_chunks, int n_comp, int n_lr) {
-    const int lane = threadIdx.x & 31;
-    const int warps = gridDim.x * (blockDim.x >> 5);
-    for (int wi = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); wi < n_a; wi += warps) {
-        const LowRankDesc d = A.lr[__ldg(A.a_order + wi)];
-        // Block exponent: max chunk exponent over the block's columns.
-        const int c_first = d.col0 / kChunk, c_last = (d.col0 + d.n - 1) / kChunk;
-        for (int p = 0; p < rhs; ++p) {
-            int eb = 0;
-            for (int c = c_first + lane; c <= c_last; c += 32) eb = max(eb, __ldg(W.xexp + p * n_chunks + c));
-            eb = __reduce_max_sync(0xFFFFFFFFu, eb);
-            const long long* Xp = W.X + (long long)p * n;
-            const int* Ep = W.xexp + p * n_chunks;
-            for (int g = 0; g < d.rank; g += 8) {
-                const int gcount = min(8, d.rank - g);
-                long long H[8], L[8];
+// sum_{e<NE} code_e * X_e for NE codes held in registers w[], decoded as
+// consumed.
+template <int W, int NE>
+__device__ __forceinline__ void codes_mac(const uint32_t* w, const int2* sX, long long& alo, long long& ahi) {
 #pragma unroll
-                for (int jj = 0; jj < 8; ++jj) H[jj] = L[jj] = 0;
-                int wj[8];
-                uint32_t oj[8];
+    for (int e = 0; e < NE; ++e) {
+        const int c = code_at<W>(w, e);
+        const int2 xx = sX[e];
+        alo += (long long)c * xx.x;
+        ahi += (long long)c * xx.y;
+    }
+}
+
+// One 32-entry chunk of a column task from a stage: lane l's words are
+// st.words[v * count + l].  Widths above 16 in two halves of 16 codes.
+template <int W>
+__device__ __forceinline__ void column_chunk(const uint32_t* sw, int count, int lane, const int2* sX,
+                                             long long& alo, long long& ahi) {
+    const uint32_t* base = sw + lane;
+    if constexpr (W <= 16 || (W & 1)) {
+        uint32_t w[W];
 #pragma unroll
-                for (int jj = 0; jj < 8; ++jj) {
-                    const int c = d.comp0 + g + min(jj, gcount - 1);
-                    wj[jj] = __ldg(A.comp_w + c);
-                    oj[jj] = __ldg(A.comp_qoff + c);
-                }
-                for (int k0 = 0; k0 < d.n; k0 += 32 * kFoldEvery) {
-                    long long ahi[8], alo[8];
+        for (int v = 0; v < W; ++v) w[v] = base[v * count];
+        codes_mac<W, 32>(w, sX, alo, ahi);
+    } else {
 #pragma unroll
-                    for (int jj = 0; jj < 8; ++jj) ahi[jj] = alo[jj] = 0;
-                    const int k1 = min(d.n, k0 + 32 * kFoldEvery);
-                    for (int k = k0 + lane; k < k1; k += 32) {
-                        const int col = d.col0 + k;
-                        long long X = Xp[col];
-                        const int sh = eb - Ep[col / kChunk];
-                        X = sh >= 63 ? 0 : (sh > 0 ? ((X + (1LL << (sh - 1))) >> sh) : X);
-                        const int xl = int(X & kLimbMask);
-                        const int xh = int(X >> kLimb);
+        for (int h = 0; h < 2; ++h) {
+            uint32_t w[W / 2];
 #pragma unroll
-                        for (int jj = 0; jj < 8; ++jj) {
-                            if (jj < gcount) {
-                                const int code = extract_code(A.qwords, oj[jj], k, wj[jj]);
-                                alo[jj] += (long long)code * xl;
-                                ahi[jj] += (long long)code * xh;
-                            }
-                        }
+            for (int v = 0; v < W / 2; ++v) w[v] = base[(h * (W / 2) + v) * count];
+            codes_mac<W, 16>(w, sX + 16 * h, alo, ahi);
+        }
+    }
+}
+
+__device__ __noinline__ void column_chunk_any(const uint32_t* sw, int W, int count, int lane, const int2* sX,
+                                              long long* a2) {
+    long long alo = 0, ahi = 0;
+    for (int e = 0; e < 32; ++e) {
+        const int pos = e * W, wi = pos >> 5, off = pos & 31;
+        const uint32_t lo = sw[wi * count + lane];
+        const uint32_t hi = off + W > 32 ? sw[(wi + 1) * count + lane] : 0u;
+        const uint32_t r = __funnelshift_r(lo, hi, off);
+        const int c = W == 32 ? int(r) : (int(r << (32 - W)) >> (32 - W));
+        const int2 xx = sX[e];
+        alo += (long long)c * xx.x;
+        ahi += (long long)c * xx.y;
+    }
+    a2[0] = alo;
+    a2[1] = ahi;
+}
+
+// Descriptor fields of one column unit, kept one per lane.
+struct ColDesc {
+    long long word0;
+    int col0, n, width, count, stride, comp_idx, chunk0, nchunks, part, nparts, split_id;
+};
+
+__device__ __forceinline__ ColDesc shfl_desc(const ColDesc& d, int src) {
+    ColDesc r;
+    r.word0 = __shfl_sync(0xFFFFFFFFu, d.word0, src);
+    r.col0 = __shfl_sync(0xFFFFFFFFu, d.col0, src);
+    r.n = __shfl_sync(0xFFFFFFFFu, d.n, src);
+    r.width = __shfl_sync(0xFFFFFFFFu, d.width, src);
+    r.count = __shfl_sync(0xFFFFFFFFu, d.count, src);
+    r.stride = __shfl_sync(0xFFFFFFFFu, d.stride, src);
+    r.comp_idx = __shfl_sync(0xFFFFFFFFu, d.comp_idx, src);
+    r.chunk0 = __shfl_sync(0xFFFFFFFFu, d.chunk0, src);
+    r.nchunks = __shfl_sync(0xFFFFFFFFu, d.nchunks, src);
+    r.part = __shfl_sync(0xFFFFFFFFu, d.part, src);
+    r.nparts = __shfl_sync(0xFFFFFFFFu, d.nparts, src);
+    r.split_id = __shfl_sync(0xFFFFFFFFu, d.split_id, src);
+    return r;
+}
+
+// Column side.  Warp gw owns units gw, gw + G, ... (heaviest first); its work
+// is the sequence (unit, rhs column, chunk), streamed through a kStages-deep
+// cp.async pipeline: chunk words and the chunk's 32 x entries are copied to
+// shared memory kStages - 1 steps ahead of their use.  Lane l accumulates
+// component l of the unit exactly; a unit's last chunk converts the sum (or,
+// for a split task, hands it to the part that finishes last).
+__global__ void __launch_bounds__(kWarps * 32, 2) column_kernel(Arena A, Work W, int n_tasks, int n, int rhs,
+                                                                int n_comp, int max_parts) {
+    extern __shared__ __align__(16) uint8_t smem_raw[];
+    __shared__ int2 sXall[kWarps][kColChunk];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    Stage* st = reinterpret_cast<Stage*>(smem_raw) + warp * kStages;
+    int2* sX = sXall[warp];
+    const int G = gridDim.x * kWarps;
+    const int gw = blockIdx.x * kWarps + warp;
+    const int my_units = gw < n_tasks ? (n_tasks - gw + G - 1) / G : 0;
+    for (int b0 = 0; b0 < my_units; b0 += 32) {
+        const int nb = min(32, my_units - b0);
+        ColDesc mine{};
+        if (lane < nb) {
+            const ColTask T = A.tasks[gw + (b0 + lane) * G];
+            mine = {T.word0, T.col0, T.n, T.width, T.count, T.stride, T.comp_idx, T.chunk0, T.nchunks,
+                    T.part, T.nparts, T.split_id};
+        }
+        // sequence cursor helpers: step s -> (unit k, column p, chunk c)
+        int total = 0;  // total steps in this batch
+        for (int k = 0; k < nb; ++k) total += rhs * __shfl_sync(0xFFFFFFFFu, mine.nchunks, k);
+        int ik = 0, ip = 0, ic = 0;  // issue cursor
+        ColDesc di = shfl_desc(mine, 0);
+        auto issue = [&](int step) {
+            if (step < total) {
+                Stage& S = st[step % kStages];
+                const uint32_t* src = A.qwords + di.word0 + (long long)(di.chunk0 + ic) * di.stride;
+                const int n16 = (di.count * di.width + 3) >> 2;
+                for (int i = lane; i < n16; i += 32) cp_async16(S.words + 4 * i, src + 4 * i);
+                const int k = (di.chunk0 + ic) * kColChunk + lane;
+                if (k < di.n) cp_async8(&S.v[lane], W.xc + (long long)ip * n + di.col0 + k);
+                // advance the issue cursor
+                if (++ic == di.nchunks) {
+                    ic = 0;
+                    if (++ip == rhs) {
+                        ip = 0;
+                        if (++ik < nb) di = shfl_desc(mine, ik);
                     }
-#pragma unroll
-                    for (int jj = 0; jj < 8; ++jj) fold(ahi[jj], alo[jj], H[jj], L[jj]);
                 }
-                // Transposed reduction: 8 (H, L) pairs over 32 lanes.
-                {
-                    const bool b4 = lane & 16;
-#pragma unroll
-                    for (int i = 0; i < 4; ++i) {
-                        const long long sh_ = b4 ? H[i] : H[i + 4], sl = b4 ? L[i] : L[i + 4];
-                        const long long rh = __shfl_xor_sync(0xFFFFFFFFu, sh_, 16);
-                        const long long rl = __shfl_xor_sync(0xFFFFFFFFu, sl, 16);
-                        H[i] = (b4 ? H[i + 4] : H[i]) + rh;
-                        L[i] = (b4 ? L[i + 4] : L[i]) + rl;
-                    }
-                    const bool b3 = lane & 8;
-#pragma unroll
-                    for (int i = 0; i < 2; ++i) {
-                        const long long sh_ = b3 ? H[i] : H[i + 2], sl = b3 ? L[i] : L[i + 2];
-                        const long long rh = __shfl_xor_sync(0xFFFFFFFFu, sh_, 8);
-                        const long long rl = __shfl_xor_sync(0xFFFFFFFFu, sl, 8);
-                        H[i] = (b3 ? H[i + 2] : H[i]) + rh;
-                        L[i] = (b3 ? L[i + 2] : L[i]) + rl;
-                    }
-                    const bool b2 = lane & 4;
-                    {
-                        const long long sh_ = b2 ? H[0] : H[1], sl = b2 ? L[0] : L[1];
-                        const long long rh = __shfl_xor_sync(0xFFFFFFFFu, sh_, 4);
-                        const long long rl = __shfl_xor_sync(0xFFFFFFFFu, sl, 4);
-                        H[0] = (b2 ? H[1] : H[0]) + rh;
-                        L[0] = (b2 ? L[1] : L[0]) + rl;
-                    }
-                    H[0] += __shfl_xor_sync(0xFFFFFFFFu, H[0], 2);
-                    L[0] += __shfl_xor_sync(0xFFFFFFFFu, L[0], 2);
-                    H[0] += __shfl_xor_sync(0xFFFFFFFFu, H[0], 1);
-                    L[0] += __shfl_xor_sync(0xFFFFFFFFu, L[0], 1);
-                }
-                const int jj = lane >> 2;  // component held by this lane
-                if ((lane & 3) == 0 && jj < gcount) {
-                    const int c = d.comp0 + g + jj;
-                    // x ~= X * 2^(eb - 1022 - kFixBits) after alignment.
-                    const double t = scalbn(two_word_to_double(H[0], L[0]), eb - 1022 - kFixBits);
-                    W.u[(long long)p * n_comp + c] = t * __ldg(A.comp_s + c);
-                }
+            }
+            cp_commit();
+        };
+#pragma unroll 1
+        for (int s = 0; s < kStages - 1; ++s) issue(s);
+        int ck = 0, cp = 0, cc = 0;  // compute cursor
+        ColDesc dc = shfl_desc(mine, 0);
+        __int128 acc = 0;
+        int xe = W.xe[0];
+        for (int step = 0; step < total; ++step) {
+            issue(step + kStages - 1);
+            cp_wait<kStages - 1>();
+            __syncwarp();
+            const Stage& S = st[step % kStages];
+            // x entries of the chunk on the column's exponent, as limbs
+            {
+                const int k = (dc.chunk0 + cc) * kColChunk + lane;
+                long long X = 0;
+                if (k < dc.n && xe) X = to_fixed(S.v[lane], xe);
+                sX[lane] = make_int2(int(X & kLimbMask), int(X >> kLimb));
             }
             __syncwarp();
-            // The block's u on one fixed-point exponent (its largest |u_bj|).
-            double* up = W.u + (long long)p * n_comp + d.comp0;
-            int e = 0;
-            for (int j = lane; j < d.rank; j += 32) e = max(e, exp_field(up[j]));
-            e = __reduce_max_sync(0xFFFFFFFFu, e);
-            int2* Up = W.U + (long long)p * n_comp + d.comp0;
-            for (int j = lane; j < d.rank; j += 32) {
-                const long long v = e ? to_fixed(up[j], e) : 0;
-                Up[j] = make_int2(int(v & kLimbMask), int(v >> kLimb));
-            }
-            if (lane == 0) W.ub[(long long)p * n_lr + __ldg(A.a_order + wi)] = e;
-        }
-    }
-}
-
-// Row side: one CTA of kTileRows threads per row tile; thread t owns clustered
-// row tile.row0 + t.  For each low-rank block covering the tile the row's
-// sum_j cP_ij U_bj is formed exactly (U_bj on the block's own exponent), then
-// shifted onto the tile's exponent (largest block exponent, kGuard guard
-// bits) and added into a 128-bit accumulator.  Dense diagonal rows are FP64.
-__global__ void __launch_bounds__(kTileRows) row_kernel(Arena A, Work W, const double* __restrict__ x,
-                                                        double* __restrict__ y, int n, int rhs,
-                                                        int n_comp, int n_lr) {
-    __shared__ int s_emax[kTileRows / 32];
-    const RowTile T = A.tiles[blockIdx.x];
-    const int t = threadIdx.x;
-    const bool active = t < T.rows;
-    const int row = T.row0 + t;
-    for (int p = 0; p < rhs; ++p) {
-        const int* ub = W.ub + (long long)p * n_lr;
-        const int2* Up = W.U + (long long)p * n_comp;
-        // 1. tile exponent: the largest block exponent among the tile's items.
-        int emax = 0;
-        for (int it = T.item0 + t; it < T.item1; it += blockDim.x) {
-            const int item = __ldg(A.items + it);
-            if (item >= 0 && A.lr[item].rank > 0) emax = max(emax, ub[item]);
-        }
-        emax = __reduce_max_sync(0xFFFFFFFFu, emax);
-        if ((t & 31) == 0) s_emax[t >> 5] = emax;
-        __syncthreads();
-        emax = 0;
-        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) emax = max(emax, s_emax[i]);
-        // 2. accumulate.
-        __int128 acc = 0;
-        double diag = 0.0;
-        for (int it = T.item0; it < T.item1; ++it) {
-            const int item = __ldg(A.items + it);
-            if (!active) continue;
-            if (item >= 0) {
-                const LowRankDesc d = A.lr[item];
-                if (d.rank == 0) continue;
-                const int rloc = row - d.row0;
-                __int128 vb = 0;
-                long long ahi = 0, alo = 0;
-                int cnt = 0;
-                for (int j = 0; j < d.rank; ++j) {
-                    const int c = d.comp0 + j;
-                    const int code = extract_code(A.pwords, __ldg(A.comp_poff + c), rloc, __ldg(A.comp_w + c));
-                    const int2 U = Up[c];
-                    alo += (long long)code * U.x;
-                    ahi += (long long)code * U.y;
-                    if (++cnt == kFoldEvery) {
-                        vb += ((__int128)ahi << kLimb) + alo;
-                        ahi = alo = 0;
-                        cnt = 0;
+            if (lane < dc.count) {
+                long long alo = 0, ahi = 0;
+                switch (dc.width) {
+                    case 4: column_chunk<4>(S.words, dc.count, lane, sX, alo, ahi); break;
+                    case 8: column_chunk<8>(S.words, dc.count, lane, sX, alo, ahi); break;
+                    case 12: column_chunk<12>(S.words, dc.count, lane, sX, alo, ahi); break;
+                    case 16: column_chunk<16>(S.words, dc.count, lane, sX, alo, ahi); break;
+                    case 24: column_chunk<24>(S.words, dc.count, lane, sX, alo, ahi); break;
+                    case 32: column_chunk<32>(S.words, dc.count, lane, sX, alo, ahi); break;
+                    default: {
+                        long long a2[2];
+                        column_chunk_any(S.words, dc.width, dc.count, lane, sX, a2);
+                        alo = a2[0];
+                        ahi = a2[1];
                     }
                 }
-                vb += ((__int128)ahi << kLimb) + alo;
-                const int sh = (emax - ub[item]) - kGuard;
-                if (sh <= 0) acc += vb << (-sh);
-                else if (sh < 127) acc += (vb + ((__int128)1 << (sh - 1))) >> sh;
-            } else {
-                const DenseDesc d = A.dd[-1 - item];
-                const double* Drow = A.dense + d.off + (long long)(row - d.row0) * d.n;
-                for (int k = 0; k < d.n; ++k)
-                    diag = fma(__ldg(Drow + k), __ldg(x + (long long)__ldg(A.perm + d.col0 + k) * rhs + p), diag);
+                acc += widen(ahi, alo);
+            }
+            __syncwarp();
+            if (++cc == dc.nchunks) {
+                // finished (unit ck, column cp)
+                if (dc.nparts == 1) {
+                    if (lane < dc.count) {
+                        const int c = __ldg(A.task_comp + dc.comp_idx + lane);
+                        const double t = xe ? scalbn(i128_to_double(acc), xe - 1022 - kFixBits) : 0.0;
+                        W.u[(long long)cp * n_comp + c] = t * __ldg(A.comp_s + c);
+                    }
+                } else {
+                    long long* part = W.part + (((long long)dc.split_id * max_parts + dc.part) * rhs + cp) * 64;
+                    part[2 * lane] = (long long)acc;
+                    part[2 * lane + 1] = (long long)(acc >> 64);
+                    __threadfence();
+                    __syncwarp();
+                    int done = 0;
+                    if (lane == 0) done = atomicAdd(W.split_cnt + (long long)dc.split_id * rhs + cp, 1);
+                    done = __shfl_sync(0xFFFFFFFFu, done, 0);
+                    if (done == dc.nparts - 1) {
+                        __threadfence();
+                        __int128 tot = 0;
+                        for (int q = 0; q < dc.nparts; ++q) {
+                            const long long* pq =
+                                W.part + (((long long)dc.split_id * max_parts + q) * rhs + cp) * 64;
+                            const unsigned long long lo = __ldcg((const unsigned long long*)pq + 2 * lane);
+                            const long long hi = __ldcg(pq + 2 * lane + 1);
+                            tot += ((__int128)hi << 64) | lo;
+                        }
+                        if (lane < dc.count) {
+                            const int c = __ldg(A.task_comp + dc.comp_idx + lane);
+                            const double t = xe ? scalbn(i128_to_double(tot), xe - 1022 - kFixBits) : 0.0;
+                            W.u[(long long)cp * n_comp + c] = t * __ldg(A.comp_s + c);
+                        }
+                    }
+                }
+                acc = 0;
+                cc = 0;
+                if (++cp == rhs) {
+                    cp = 0;
+                    if (++ck < nb) dc = shfl_desc(mine, ck);
+                }
+                xe = W.xe[cp];
             }
         }
-        if (active) {
-            double lr = 0.0;
-            if (emax) {
-                const long long hi = (long long)(acc >> 64);
-                const unsigned long long lo = (unsigned long long)acc;
-                lr = scalbn(fma(double(hi), 18446744073709551616.0, double(lo)), emax - 1022 - kFixBits - kGuard);
+        cp_wait<0>();
+        __syncwarp();
+    }
+}
+
+// Lanes whose first row lies past the tile read nothing.
+template <int WID>
+__device__ __forceinline__ void row_component(const uint32_t* piece, int lane, bool active, int ul, int uh,
+                                              long long& alo0, long long& ahi0, long long& alo1, long long& ahi1) {
+    int c0 = 0, c1 = 0;
+    if (active) row_pair_codes<WID>(piece, lane, c0, c1);
+    alo0 += (long long)c0 * ul;
+    ahi0 += (long long)c0 * uh;
+    alo1 += (long long)c1 * ul;
+    ahi1 += (long long)c1 * uh;
+}
+
+// acc (on exponent e_acc, kGuard guard bits) += v (on exponent ev); the
+// accumulator's exponent rises to ev first if ev is larger.
+__device__ __forceinline__ void add_aligned(__int128& acc0, __int128& acc1, int& e_acc, __int128 v0, __int128 v1,
+                                            int ev) {
+    if (ev > e_acc) {
+        const int d = ev - e_acc;
+        if (d >= 127) {
+            acc0 = acc1 = 0;
+        } else {
+            const __int128 half = (__int128)1 << (d - 1);
+            acc0 = (acc0 + half) >> d;
+            acc1 = (acc1 + half) >> d;
+        }
+        e_acc = ev;
+    }
+    const int sh = (e_acc - ev) - kGuard;
+    if (sh <= 0) {
+        acc0 += v0 << (-sh);
+        acc1 += v1 << (-sh);
+    } else if (sh < 127) {
+        const __int128 half = (__int128)1 << (sh - 1);
+        acc0 += (v0 + half) >> sh;
+        acc1 += (v1 + half) >> sh;
+    }
+}
+
+struct RowDesc {
+    int block, rloc0, comp, count, words;
+    long long off;
+};
+
+// Row side: one CTA of kWarps warps per row tile; warp w owns the tile's
+// units w, w + kWarps, ...; lane l owns tile rows 2l and 2l + 1.  Each warp
+// streams its units (for every rhs column) through a kStages-deep cp.async
+// pipeline (a unit's data block and its components' u values).  A unit's
+// u are put in fixed point on the unit's own exponent, its row sums are exact,
+// and they are added into 128-bit row accumulators kept on a running exponent
+// with kGuard guard bits.  Dense diagonal units use FP64 loads directly.
+// Warps combine per rhs column in shared memory in a fixed order.
+__global__ void __launch_bounds__(kWarps * 32, 2) row_kernel(Arena A, Work W, double* __restrict__ y,
+                                                             int n, int rhs, int n_comp) {
+    extern __shared__ __align__(16) uint8_t smem_raw[];
+    __shared__ __int128 s_acc[kWarps][kTileRows];
+    __shared__ int s_e[kWarps];
+    __shared__ double s_diag[kTileRows];
+    __shared__ int s_has_diag;
+    const RowTile T = A.tiles[blockIdx.x];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    Stage* st = reinterpret_cast<Stage*>(smem_raw) + warp * kStages;
+    const int r0 = 2 * lane, r1 = 2 * lane + 1;
+    const int nunits = T.item1 - T.item0;
+    const int my = warp < nunits ? (nunits - warp + kWarps - 1) / kWarps : 0;
+    if (threadIdx.x == 0) s_has_diag = 0;
+    __syncthreads();
+    // All of a warp's units, one per lane, in batches of 32 (units of one
+    // tile rarely exceed 32 per warp).
+    for (int p = 0; p < rhs; ++p) {
+        __int128 acc0 = 0, acc1 = 0;
+        int e_acc = 0;
+        for (int b0 = 0; b0 < my; b0 += 32) {
+            const int nb = min(32, my - b0);
+            RowDesc mine{};
+            if (lane < nb) {
+                const RowItem I = A.items[T.item0 + warp + (b0 + lane) * kWarps];
+                mine = {I.block, I.rloc0, I.comp, I.count, I.words, I.off};
             }
-            y[(long long)__ldg(A.perm + row) * rhs + p] = diag + lr;
+            auto desc = [&](int k) {
+                RowDesc d;
+                d.block = __shfl_sync(0xFFFFFFFFu, mine.block, k);
+                d.rloc0 = __shfl_sync(0xFFFFFFFFu, mine.rloc0, k);
+                d.comp = __shfl_sync(0xFFFFFFFFu, mine.comp, k);
+                d.count = __shfl_sync(0xFFFFFFFFu, mine.count, k);
+                d.words = __shfl_sync(0xFFFFFFFFu, mine.words, k);
+                d.off = __shfl_sync(0xFFFFFFFFu, mine.off, k);
+                return d;
+            };
+            auto issue = [&](int k) {
+                if (k < nb) {
+                    const RowDesc d = desc(k);
+                    if (d.block >= 0) {
+                        Stage& S = st[k % kStages];
+                        const uint32_t* src = A.pwords + d.off;
+                        for (int i = lane; i < (d.words >> 2); i += 32) cp_async16(S.words + 4 * i, src + 4 * i);
+                        if (lane < d.count) cp_async8(&S.v[lane], W.u + (long long)p * n_comp + d.comp + lane);
+                    }
+                }
+                cp_commit();
+            };
+#pragma unroll 1
+            for (int s = 0; s < kStages - 1; ++s) issue(s);
+            for (int k = 0; k < nb; ++k) {
+                issue(k + kStages - 1);
+                cp_wait<kStages - 1>();
+                __syncwarp();
+                const RowDesc d = desc(k);
+                const Stage& S = st[k % kStages];
+                if (d.block >= 0) {
+                    // widths from the header, u from the stage
+                    int wl = 0;
+                    double uv = 0.0;
+                    if (lane < d.count) {
+                        wl = int((S.words[lane >> 2] >> (8 * (lane & 3))) & 0xFFu);
+                        uv = S.v[lane];
+                    }
+                    const int eb = __reduce_max_sync(0xFFFFFFFFu, lane < d.count ? exp_field(uv) : 0);
+                    if (eb) {
+                        const long long U = lane < d.count ? to_fixed(uv, eb) : 0;
+                        const int ul_l = int(U & kLimbMask), uh_l = int(U >> kLimb);
+                        const int sz = (T.rows * wl + 31) >> 5;
+                        int incl = sz;
+#pragma unroll
+                        for (int o = 1; o < 32; o <<= 1) {
+                            const int v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+                            if (lane >= o) incl += v;
+                        }
+                        const int offl = kRowHeaderWords + incl - sz;
+                        long long alo0 = 0, ahi0 = 0, alo1 = 0, ahi1 = 0;
+                        const bool act = r0 < T.rows;
+                        for (int jj = 0; jj < d.count; ++jj) {
+                            const int w = __shfl_sync(0xFFFFFFFFu, wl, jj);
+                            const int ul = __shfl_sync(0xFFFFFFFFu, ul_l, jj);
+                            const int uh = __shfl_sync(0xFFFFFFFFu, uh_l, jj);
+                            const uint32_t* piece = S.words + __shfl_sync(0xFFFFFFFFu, offl, jj);
+                            switch (w) {
+#define QH_ROW_CASE(WW) \
+    case WW:            \
+        row_component<WW>(piece, lane, act, ul, uh, alo0, ahi0, alo1, ahi1); \
+        break;
+                                QH_WIDTH_CASES(QH_ROW_CASE)
+#undef QH_ROW_CASE
+                                default:
+                                    break;
+                            }
+                        }
+                        __int128 v0 = widen(ahi0, alo0), v1 = widen(ahi1, alo1);
+                        if (r0 >= T.rows) v0 = 0;
+                        if (r1 >= T.rows) v1 = 0;
+                        add_aligned(acc0, acc1, e_acc, v0, v1, eb);
+                    }
+                } else {
+                    // dense diagonal block (at most one per tile), column-major values
+                    const DenseDesc dd = A.dd[-1 - d.block];
+                    const double* D = A.dense + d.off;
+                    const double* xcp = W.xc + (long long)p * n + dd.col0;
+                    double dg0 = 0.0, dg1 = 0.0;
+                    const bool v0 = r0 < T.rows, v1 = r1 < T.rows;
+#pragma unroll 4
+                    for (int kk = 0; kk < dd.n; ++kk) {
+                        const double xk = __ldg(xcp + kk);
+                        const double* col = D + (long long)kk * dd.m;
+                        if (v0) dg0 = fma(__ldg(col + r0), xk, dg0);
+                        if (v1) dg1 = fma(__ldg(col + r1), xk, dg1);
+                    }
+                    s_diag[r0] = dg0;
+                    s_diag[r1] = dg1;
+                    s_has_diag = 1;
+                }
+                __syncwarp();
+            }
+            cp_wait<0>();
+            __syncwarp();
+        }
+        s_acc[warp][r0] = acc0;
+        s_acc[warp][r1] = acc1;
+        if (lane == 0) s_e[warp] = e_acc;
+        __syncthreads();
+        if (threadIdx.x < T.rows) {
+            const int r = threadIdx.x;
+            int et = 0;
+#pragma unroll
+            for (int i = 0; i < kWarps; ++i) et = max(et, s_e[i]);
+            __int128 tot = 0;
+#pragma unroll
+            for (int i = 0; i < kWarps; ++i) {
+                const int dsh = et - s_e[i];
+                const __int128 a = s_acc[i][r];
+                if (dsh == 0) tot += a;
+                else if (dsh < 127) tot += (a + ((__int128)1 << (dsh - 1))) >> dsh;
+            }
+            const double lr = et ? scalbn(i128_to_double(tot), et - 1022 - kFixBits - kGuard) : 0.0;
+            const double dg = s_has_diag ? s_diag[r] : 0.0;
+            y[(long long)__ldg(A.perm + T.row0 + r) * rhs + p] = dg + lr;
         }
         __syncthreads();
     }
 }
 
-// Validation: decode every code of one side, one warp per component.
-__global__ void decode_kernel(Arena A, int side, int n_lr, const long long* __restrict__ out_off,
-                              int* __restrict__ out) {
+// Validation: decode every code through the same device routines the apply
+// kernels use (code_at / row_pair_codes on the resident layout).  Column
+// side: one warp per unit; row side: one warp per tile.
+template <int W>
+__device__ __forceinline__ void col_codes(const uint32_t* cw, int count, int lane, int (&c)[32]) {
+    uint32_t w[W];
+#pragma unroll
+    for (int v = 0; v < W; ++v) w[v] = cw[v * count + lane];
+#pragma unroll
+    for (int e = 0; e < 32; ++e) c[e] = code_at<W>(w, e);
+}
+
+__global__ void decode_col_kernel(Arena A, int n_tasks, const long long* __restrict__ comp_off, int* out) {
     const int lane = threadIdx.x & 31;
     const int warps = gridDim.x * (blockDim.x >> 5);
-    for (int b = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); b < n_lr; b += warps) {
-        const LowRankDesc d = A.lr[b];
-        const int rows = side == 0 ? d.m : d.n;
-        const uint32_t* words = side == 0 ? A.pwords : A.qwords;
-        const uint32_t* offs = side == 0 ? A.comp_poff : A.comp_qoff;
-        long long o = out_off[b];
-        for (int j = 0; j < d.rank; ++j) {
-            const int c = d.comp0 + j;
-            for (int i = lane; i < rows; i += 32) out[o + i] = extract_code(words, offs[c], i, A.comp_w[c]);
-            o += rows;
+    for (int ti = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); ti < n_tasks; ti += warps) {
+        const ColTask T = A.tasks[ti];
+        if (lane >= T.count) continue;
+        const long long o = comp_off[__ldg(A.task_comp + T.comp_idx + lane)];
+        for (int ch = T.chunk0; ch < T.chunk0 + T.nchunks; ++ch) {
+            const uint32_t* cw = A.qwords + T.word0 + (long long)ch * T.stride;
+            int c[32];
+            switch (T.width) {
+#define QH_DEC_CASE(WW) \
+    case WW:            \
+        col_codes<WW>(cw, T.count, lane, c); \
+        break;
+                QH_WIDTH_CASES(QH_DEC_CASE)
+#undef QH_DEC_CASE
+                default:
+                    break;
+            }
+            for (int e = 0; e < 32; ++e)
+                if (ch * kColChunk + e < T.n) out[o + ch * kColChunk + e] = c[e];
+        }
+    }
+}
+
+__global__ void decode_row_kernel(Arena A, int n_tiles, const long long* __restrict__ comp_off, int* out) {
+    const int lane = threadIdx.x & 31;
+    const int warps = gridDim.x * (blockDim.x >> 5);
+    for (int t = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); t < n_tiles; t += warps) {
+        const RowTile T = A.tiles[t];
+        for (int it = T.item0; it < T.item1; ++it) {
+            const RowItem I = A.items[it];
+            if (I.block < 0) continue;
+            const uint32_t* blk = A.pwords + I.off;
+            const uint32_t* piece = blk + kRowHeaderWords;
+            for (int j = 0; j < I.count; ++j) {
+                const int w = int((blk[j >> 2] >> (8 * (j & 3))) & 0xFFu);
+                int c0 = 0, c1 = 0;
+                switch (2 * lane < T.rows ? w : 0) {
+#define QH_DEC_CASE(WW)                                \
+    case WW:                                           \
+        row_pair_codes<WW>(piece, lane, c0, c1);       \
+        break;
+                    QH_WIDTH_CASES(QH_DEC_CASE)
+#undef QH_DEC_CASE
+                    default:
+                        break;
+                }
+                const long long o = comp_off[I.comp + j] + I.rloc0;
+                if (2 * lane < T.rows) out[o + 2 * lane] = c0;
+                if (2 * lane + 1 < T.rows) out[o + 2 * lane + 1] = c1;
+                piece += (T.rows * w + 31) >> 5;
+            }
         }
     }
 }
@@ -448,6 +804,13 @@ int upload(Layout&& L, int device, qh_matrix** out) {
         return cuda_fail(e, "cudaMemcpy host-to-device");
     }
     cudaDeviceGetAttribute(&m->sms, cudaDevAttrMultiProcessorCount, device);
+    e = cudaFuncSetAttribute(row_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kPipeSmem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(column_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kPipeSmem);
+    if (e != cudaSuccess) {
+        delete m;
+        return cuda_fail(e, "cudaFuncSetAttribute");
+    }
     // The host image is no longer needed once uploaded.
     std::vector<uint8_t>().swap(m->L.arena);
     const Sections& S = m->L.sec;
@@ -457,14 +820,13 @@ int upload(Layout&& L, int device, qh_matrix** out) {
     m->A.dd = reinterpret_cast<const DenseDesc*>(base + S.dd);
     m->A.comp_w = base + S.comp_w;
     m->A.comp_s = reinterpret_cast<const double*>(base + S.comp_s);
-    m->A.comp_qoff = reinterpret_cast<const uint32_t*>(base + S.comp_qoff);
-    m->A.comp_poff = reinterpret_cast<const uint32_t*>(base + S.comp_poff);
+    m->A.tasks = reinterpret_cast<const ColTask*>(base + S.tasks);
+    m->A.task_comp = reinterpret_cast<const int32_t*>(base + S.task_comp);
     m->A.qwords = reinterpret_cast<const uint32_t*>(base + S.qwords);
     m->A.pwords = reinterpret_cast<const uint32_t*>(base + S.pwords);
     m->A.dense = reinterpret_cast<const double*>(base + S.dense);
-    m->A.a_order = reinterpret_cast<const int32_t*>(base + S.a_order);
     m->A.tiles = reinterpret_cast<const RowTile*>(base + S.tiles);
-    m->A.items = reinterpret_cast<const int32_t*>(base + S.items);
+    m->A.items = reinterpret_cast<const RowItem*>(base + S.items);
     *out = m;
     return QH_OK;
 }
@@ -485,7 +847,7 @@ int guarded(F&& f) {
 }
 
 struct WsPlan {
-    size_t X, xexp, u, U, ub, total;
+    size_t xc, xe, cnt, part, u, total, zero_bytes;
 };
 
 WsPlan ws_plan(const Layout& L, size_t rhs) {
@@ -496,11 +858,13 @@ WsPlan ws_plan(const Layout& L, size_t rhs) {
         off += align256(std::max<size_t>(bytes, 1));
         return o;
     };
-    w.X = take(8 * L.order * rhs);
-    w.xexp = take(4 * size_t(L.n_chunks) * rhs);
+    // zeroed before each apply: xe and the split counters (contiguous)
+    w.xe = take(4 * rhs);
+    w.cnt = take(4 * size_t(L.n_split) * rhs);
+    w.zero_bytes = off;
+    w.xc = take(8 * L.order * rhs);
+    w.part = take(16 * 32 * size_t(L.n_split) * size_t(L.max_parts) * rhs);
     w.u = take(8 * size_t(L.n_comp) * rhs);
-    w.U = take(8 * size_t(L.n_comp) * rhs);
-    w.ub = take(4 * size_t(L.n_lr) * rhs);
     w.total = off;
     return w;
 }
@@ -514,26 +878,28 @@ int launch(const qh_matrix* m, const double* x, double* y, size_t rhs, void* ws,
     auto* w = static_cast<uint8_t*>(ws);
     const WsPlan P = ws_plan(L, rhs);
     Work W;
-    W.X = reinterpret_cast<long long*>(w + P.X);
-    W.xexp = reinterpret_cast<int*>(w + P.xexp);
+    W.xc = reinterpret_cast<double*>(w + P.xc);
+    W.xe = reinterpret_cast<int*>(w + P.xe);
+    W.split_cnt = reinterpret_cast<int*>(w + P.cnt);
+    W.part = reinterpret_cast<long long*>(w + P.part);
     W.u = reinterpret_cast<double*>(w + P.u);
-    W.U = reinterpret_cast<int2*>(w + P.U);
-    W.ub = reinterpret_cast<int*>(w + P.ub);
     auto mark = [&](int i) {
         if (ev) cudaEventRecord(static_cast<cudaEvent_t>(ev[i]), s);
     };
     const long long prep_warps = (long long)L.n_chunks * (long long)rhs;
     mark(0);
+    cudaError_t e = cudaMemsetAsync(w, 0, P.zero_bytes, s);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
     prep_x_kernel<<<unsigned((prep_warps + 7) / 8), 256, 0, s>>>(m->A, W, x, n, int(rhs), L.n_chunks, status);
     mark(1);
-    if (L.n_a > 0) {
-        const int grid = std::max(1, std::min((L.n_a + 7) / 8, m->sms * 8));
-        column_kernel<<<grid, 256, 0, s>>>(m->A, W, L.n_a, n, int(rhs), L.n_chunks, L.n_comp, L.n_lr);
+    if (L.n_tasks > 0) {
+        const int grid = std::max(1, std::min((L.n_tasks + kWarps - 1) / kWarps, m->sms * 2));
+        column_kernel<<<grid, kWarps * 32, kPipeSmem, s>>>(m->A, W, L.n_tasks, n, int(rhs), L.n_comp, L.max_parts);
     }
     mark(2);
-    row_kernel<<<L.n_tiles, kTileRows, 0, s>>>(m->A, W, x, y, n, int(rhs), L.n_comp, L.n_lr);
+    row_kernel<<<L.n_tiles, kWarps * 32, kPipeSmem, s>>>(m->A, W, y, n, int(rhs), L.n_comp);
     mark(3);
-    cudaError_t e = cudaGetLastError();
+    e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "CUDA kernel launch");
     return QH_OK;
 }
@@ -754,9 +1120,12 @@ int qh_debug_decode(const qh_matrix* m, int side, int32_t* out, size_t out_count
             e = cudaMemcpy(lr.data(), m->A.lr, sizeof(LowRankDesc) * lr.size(), cudaMemcpyDeviceToHost);
             if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy device-to-host");
         }
-        std::vector<long long> off(lr.size() + 1, 0);
-        for (size_t b = 0; b < lr.size(); ++b)
-            off[b + 1] = off[b] + (long long)lr[b].rank * (side == 0 ? lr[b].m : lr[b].n);
+        // component-major output: component c's codes start at off[c]
+        std::vector<long long> off(size_t(m->L.n_comp) + 1, 0);
+        for (const auto& d : lr)
+            for (int j = 0; j < d.rank; ++j)
+                off[size_t(d.comp0 + j) + 1] = side == 0 ? d.m : d.n;
+        for (size_t c = 0; c + 1 < off.size(); ++c) off[c + 1] += off[c];
         const size_t total = size_t(off.back());
         if (needed) *needed = total;
         if (!out) return QH_OK;
@@ -772,7 +1141,10 @@ int qh_debug_decode(const qh_matrix* m, int side, int32_t* out, size_t out_count
         int rc = QH_OK;
         e = cudaMemcpy(d_off, off.data(), sizeof(long long) * off.size(), cudaMemcpyHostToDevice);
         if (e == cudaSuccess) {
-            decode_kernel<<<std::max(1, std::min((m->L.n_lr + 7) / 8, 4096)), 256>>>(m->A, side, m->L.n_lr, d_off, d_out);
+            if (side == 1)
+                decode_col_kernel<<<std::max(1, std::min((m->L.n_tasks + 7) / 8, 4096)), 256>>>(m->A, m->L.n_tasks, d_off, d_out);
+            else
+                decode_row_kernel<<<std::max(1, std::min((m->L.n_tiles + 7) / 8, 4096)), 256>>>(m->A, m->L.n_tiles, d_off, d_out);
             e = cudaGetLastError();
         }
         if (e == cudaSuccess) e = cudaMemcpy(out, d_out, sizeof(int) * total, cudaMemcpyDeviceToHost);
