@@ -429,17 +429,27 @@ Layout build_layout(const HostMatrix& m) {
             const int32_t rows = int32_t(std::min<uint64_t>(kTileRows, bounds[s + 1] - r));
             RowTile T{int32_t(r), rows, int32_t(items.size()), 0};
             int64_t work = 0;
+            std::vector<std::pair<int64_t, RowItem>> units;  // (cost, unit)
             for (int32_t k : slab_blocks[s]) {
                 const auto& b = m.blocks[size_t(k)];
                 const int32_t rloc0 = int32_t(r - b.row0);
                 if (b.dense) {
-                    RowItem it{};
-                    it.block = block_item[size_t(k)];
-                    it.rloc0 = rloc0;
-                    const DenseDesc& d = dd[size_t(-1 - it.block)];
-                    it.off = d.off + rloc0;
-                    items.push_back(it);
-                    work += int64_t(rows) * d.n * 4;
+                    // column slices, one per warp, summed in slice order
+                    const DenseDesc& d = dd[size_t(-1 - block_item[size_t(k)])];
+                    const int32_t ns = std::min<int32_t>(kDenseSlices, d.n);
+                    for (int32_t sl = 0; sl < ns; ++sl) {
+                        const int32_t c0 = int32_t(int64_t(d.n) * sl / ns), c1 = int32_t(int64_t(d.n) * (sl + 1) / ns);
+                        RowItem it{};
+                        it.block = block_item[size_t(k)];
+                        it.rloc0 = rloc0;
+                        it.comp = sl;          // slice index
+                        it.count = c1 - c0;    // columns in the slice
+                        it.off = d.off + int64_t(c0) * d.m + rloc0;
+                        it.words = c0;         // first column of the slice
+                        const int64_t cost = int64_t(rows) * (c1 - c0) * 16;
+                        units.push_back({cost, it});
+                        work += cost;
+                    }
                     continue;
                 }
                 const uint64_t rows_b = b.row1 - b.row0;
@@ -472,11 +482,16 @@ Layout build_layout(const HostMatrix& m) {
                                   uint64_t(rloc0) * w, uint64_t(rows) * w, pwords.data() + o);
                         o += words_for_bits(uint64_t(rows), w);
                     }
-                    items.push_back(it);
-                    work += int64_t(rows) * int64_t(j1 - j0) + 64;
+                    const int64_t cost = int64_t(rows) * int64_t(j1 - j0) + 64;
+                    units.push_back({cost, it});
+                    work += cost;
                     j0 = j1;
                 }
             }
+            // heaviest first: the tile's warps take units round-robin
+            std::stable_sort(units.begin(), units.end(),
+                             [](const auto& a, const auto& b) { return a.first > b.first; });
+            for (const auto& u : units) items.push_back(u.second);
             T.item1 = int32_t(items.size());
             tiles.push_back(T);
             tile_work.push_back(work);

@@ -106,7 +106,9 @@ struct ColTask {
     int32_t pad;
 };
 // Row-side unit of work: components [j0, j0 + count) of one low-rank block for
-// one row tile, or one dense block for one row tile (count == 0).  Low-rank
+// one row tile, or a column slice of one dense block for one row tile (dense:
+// comp = slice index, count = columns, words = first column, off = element
+// offset of (first row, first column) in the column-major values).  Low-rank
 // data block at pwords[off]: 8 header words holding the `count` widths (one
 // byte each), then the pieces (component j's piece = bits [rloc0*w, (rloc0 +
 // rows)*w) of its run, from a fresh word, ceil(rows*w/32) words); `words` is
@@ -133,6 +135,8 @@ constexpr int kStageWordBytes = 4096;
 constexpr int kMaxPartChunks = 16;
 // Header words of a row data block (32 widths, one byte each).
 constexpr int kRowHeaderWords = 8;
+// Column slices a dense diagonal block is cut into (one per row-side warp).
+constexpr int kDenseSlices = 8;
 
 // Byte offsets of each section inside the device arena.
 struct Sections {

@@ -180,34 +180,20 @@ __device__ __forceinline__ void col_chunk_codes(const uint32_t (&w)[W], int (&c)
     for (int e = 0; e < 32; ++e) c[e] = code_at<W>(w, e);
 }
 
-// Row side: codes of rows 2*lane and 2*lane+1 of a piece (bit string of the
-// tile's rows of one component, starting at a fresh word).  `piece` may point
-// to shared or global memory.
-template <int W>
-__device__ __forceinline__ void row_pair_codes(const uint32_t* piece, int lane, int& c0, int& c1) {
-    const uint32_t pos = uint32_t(lane) * (2 * W);
+// Row side: codes of rows 2*lane and 2*lane+1 of a piece (the bit string of
+// the tile's rows of one component, from a fresh word), width W at run time.
+// No branches: three words are read and the shift amounts computed, because a
+// data-dependent branch per component stalls the warp far longer than the
+// extra arithmetic.
+__device__ __forceinline__ void row_pair_codes_rt(const uint32_t* piece, int lane, int W, int& c0, int& c1) {
+    const uint32_t pos = uint32_t(lane) * uint32_t(2 * W);
     const uint32_t wi = pos >> 5, off = pos & 31;
-    if constexpr (32 % (2 * W) == 0) {
-        // both fields inside one word
-        const uint32_t r = piece[wi] >> off;
-        c0 = sext<W>(r);
-        c1 = sext<W>(r >> W);
-    } else if constexpr (W == 32) {
-        c0 = int(piece[wi]);
-        c1 = int(piece[wi + 1]);
-    } else if constexpr (W <= 16) {
-        const uint32_t lo = piece[wi], hi = piece[wi + 1];
-        const unsigned long long r = (((unsigned long long)hi << 32) | lo) >> off;
-        c0 = sext<W>(uint32_t(r));
-        c1 = sext<W>(uint32_t(r >> W));
-    } else {
-        const uint32_t a = piece[wi], b = piece[wi + 1], d = piece[wi + 2];
-        c0 = sext<W>(__funnelshift_r(a, b, off));
-        // row 2*lane+1 starts at off + W (< 64)
-        const uint32_t p1 = off + W;
-        const uint32_t x0 = p1 < 32 ? a : b, x1 = p1 < 32 ? b : d;
-        c1 = sext<W>(__funnelshift_r(x0, x1, p1 & 31));
-    }
+    const uint32_t a = piece[wi], b = piece[wi + 1], d = piece[wi + 2];
+    const uint32_t sh = 32u - uint32_t(W);
+    c0 = int(__funnelshift_r(a, b, off) << sh) >> sh;
+    const uint32_t p1 = off + uint32_t(W);
+    const uint32_t lo = p1 < 32 ? a : b, hi = p1 < 32 ? b : d;
+    c1 = int(__funnelshift_r(lo, hi, p1 & 31) << sh) >> sh;
 }
 
 // Dispatch a width to a template instance.
@@ -240,13 +226,20 @@ __global__ void __launch_bounds__(256) prep_x_kernel(Arena A, Work W, const doub
 // consumed.
 template <int W, int NE>
 __device__ __forceinline__ void codes_mac(const uint32_t* w, const int2* sX, long long& alo, long long& ahi) {
+    // four independent accumulator pairs keep the multiply-add chains short
+    long long l[4] = {0, 0, 0, 0}, h[4] = {0, 0, 0, 0};
+    const int4* sX2 = reinterpret_cast<const int4*>(sX);
 #pragma unroll
-    for (int e = 0; e < NE; ++e) {
-        const int c = code_at<W>(w, e);
-        const int2 xx = sX[e];
-        alo += (long long)c * xx.x;
-        ahi += (long long)c * xx.y;
+    for (int e = 0; e < NE; e += 2) {
+        const int4 xx = sX2[e >> 1];
+        const int c0 = code_at<W>(w, e), c1 = code_at<W>(w, e + 1);
+        l[e & 3] += (long long)c0 * xx.x;
+        h[e & 3] += (long long)c0 * xx.y;
+        l[(e + 1) & 3] += (long long)c1 * xx.z;
+        h[(e + 1) & 3] += (long long)c1 * xx.w;
     }
+    alo += (l[0] + l[1]) + (l[2] + l[3]);
+    ahi += (h[0] + h[1]) + (h[2] + h[3]);
 }
 
 // One 32-entry chunk of a column task from a stage: lane l's words are
@@ -311,18 +304,28 @@ __device__ __forceinline__ ColDesc shfl_desc(const ColDesc& d, int src) {
     return r;
 }
 
+constexpr int kSlotBytes = int(sizeof(Stage));
+
+// Chunks of one (unit, column) that one pipeline step carries: as many as fit
+// a slot (code words plus 32 x entries per chunk), at least one.
+__device__ __forceinline__ int col_step_chunks(int stride, int remaining) {
+    const int per = stride * 4 + kColChunk * 8;
+    return max(1, min(remaining, kSlotBytes / per));
+}
+
 // Column side.  Warp gw owns units gw, gw + G, ... (heaviest first); its work
 // is the sequence (unit, rhs column, chunk), streamed through a kStages-deep
-// cp.async pipeline: chunk words and the chunk's 32 x entries are copied to
-// shared memory kStages - 1 steps ahead of their use.  Lane l accumulates
-// component l of the unit exactly; a unit's last chunk converts the sum (or,
-// for a split task, hands it to the part that finishes last).
+// cp.async pipeline whose steps carry as many chunks as fit a slot: chunk
+// words and the chunks' x entries are copied to shared memory kStages - 1
+// steps ahead of their use.  Lane l accumulates component l of the unit
+// exactly; a unit's last chunk converts the sum (or, for a split task, hands
+// it to the part that finishes last).
 __global__ void __launch_bounds__(kWarps * 32, 2) column_kernel(Arena A, Work W, int n_tasks, int n, int rhs,
                                                                 int n_comp, int max_parts) {
     extern __shared__ __align__(16) uint8_t smem_raw[];
-    __shared__ int2 sXall[kWarps][kColChunk];
+    __shared__ __align__(16) int2 sXall[kWarps][kColChunk];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    Stage* st = reinterpret_cast<Stage*>(smem_raw) + warp * kStages;
+    uint8_t* slots = smem_raw + (size_t)warp * kStages * kSlotBytes;
     int2* sX = sXall[warp];
     const int G = gridDim.x * kWarps;
     const int gw = blockIdx.x * kWarps + warp;
@@ -335,21 +338,23 @@ __global__ void __launch_bounds__(kWarps * 32, 2) column_kernel(Arena A, Work W,
             mine = {T.word0, T.col0, T.n, T.width, T.count, T.stride, T.comp_idx, T.chunk0, T.nchunks,
                     T.part, T.nparts, T.split_id};
         }
-        // sequence cursor helpers: step s -> (unit k, column p, chunk c)
-        int total = 0;  // total steps in this batch
-        for (int k = 0; k < nb; ++k) total += rhs * __shfl_sync(0xFFFFFFFFu, mine.nchunks, k);
-        int ik = 0, ip = 0, ic = 0;  // issue cursor
+        int ik = 0, ip = 0, ic = 0, issued = 0;  // issue cursor
         ColDesc di = shfl_desc(mine, 0);
-        auto issue = [&](int step) {
-            if (step < total) {
-                Stage& S = st[step % kStages];
+        auto issue = [&]() {
+            if (ik < nb) {
+                const int nc = col_step_chunks(di.stride, di.nchunks - ic);
+                uint8_t* slot = slots + (issued % kStages) * kSlotBytes;
+                uint32_t* sw = reinterpret_cast<uint32_t*>(slot);
+                double* sv = reinterpret_cast<double*>(slot + nc * di.stride * 4);
                 const uint32_t* src = A.qwords + di.word0 + (long long)(di.chunk0 + ic) * di.stride;
-                const int n16 = (di.count * di.width + 3) >> 2;
-                for (int i = lane; i < n16; i += 32) cp_async16(S.words + 4 * i, src + 4 * i);
-                const int k = (di.chunk0 + ic) * kColChunk + lane;
-                if (k < di.n) cp_async8(&S.v[lane], W.xc + (long long)ip * n + di.col0 + k);
-                // advance the issue cursor
-                if (++ic == di.nchunks) {
+                const int n16 = (nc * di.stride) >> 2;
+                for (int i = lane; i < n16; i += 32) cp_async16(sw + 4 * i, src + 4 * i);
+                for (int c = 0; c < nc; ++c) {
+                    const int k = (di.chunk0 + ic + c) * kColChunk + lane;
+                    if (k < di.n) cp_async8(sv + c * kColChunk + lane, W.xc + (long long)ip * n + di.col0 + k);
+                }
+                ic += nc;
+                if (ic == di.nchunks) {
                     ic = 0;
                     if (++ip == rhs) {
                         ip = 0;
@@ -357,47 +362,56 @@ __global__ void __launch_bounds__(kWarps * 32, 2) column_kernel(Arena A, Work W,
                     }
                 }
             }
+            ++issued;
             cp_commit();
         };
 #pragma unroll 1
-        for (int s = 0; s < kStages - 1; ++s) issue(s);
-        int ck = 0, cp = 0, cc = 0;  // compute cursor
+        for (int s = 0; s < kStages - 1; ++s) issue();
+        int ck = 0, cp = 0, cc = 0, computed = 0;  // compute cursor
         ColDesc dc = shfl_desc(mine, 0);
         __int128 acc = 0;
         int xe = W.xe[0];
-        for (int step = 0; step < total; ++step) {
-            issue(step + kStages - 1);
+        while (ck < nb) {
+            issue();
             cp_wait<kStages - 1>();
             __syncwarp();
-            const Stage& S = st[step % kStages];
-            // x entries of the chunk on the column's exponent, as limbs
-            {
-                const int k = (dc.chunk0 + cc) * kColChunk + lane;
-                long long X = 0;
-                if (k < dc.n && xe) X = to_fixed(S.v[lane], xe);
-                sX[lane] = make_int2(int(X & kLimbMask), int(X >> kLimb));
-            }
-            __syncwarp();
-            if (lane < dc.count) {
-                long long alo = 0, ahi = 0;
-                switch (dc.width) {
-                    case 4: column_chunk<4>(S.words, dc.count, lane, sX, alo, ahi); break;
-                    case 8: column_chunk<8>(S.words, dc.count, lane, sX, alo, ahi); break;
-                    case 12: column_chunk<12>(S.words, dc.count, lane, sX, alo, ahi); break;
-                    case 16: column_chunk<16>(S.words, dc.count, lane, sX, alo, ahi); break;
-                    case 24: column_chunk<24>(S.words, dc.count, lane, sX, alo, ahi); break;
-                    case 32: column_chunk<32>(S.words, dc.count, lane, sX, alo, ahi); break;
-                    default: {
-                        long long a2[2];
-                        column_chunk_any(S.words, dc.width, dc.count, lane, sX, a2);
-                        alo = a2[0];
-                        ahi = a2[1];
-                    }
+            const int nc = col_step_chunks(dc.stride, dc.nchunks - cc);
+            const uint8_t* slot = slots + (computed % kStages) * kSlotBytes;
+            const uint32_t* sw = reinterpret_cast<const uint32_t*>(slot);
+            const double* sv = reinterpret_cast<const double*>(slot + nc * dc.stride * 4);
+            for (int c = 0; c < nc; ++c) {
+                // the chunk's x entries on the column's exponent, as limbs
+                {
+                    const int k = (dc.chunk0 + cc + c) * kColChunk + lane;
+                    long long X = 0;
+                    if (k < dc.n && xe) X = to_fixed(sv[c * kColChunk + lane], xe);
+                    sX[lane] = make_int2(int(X & kLimbMask), int(X >> kLimb));
                 }
-                acc += widen(ahi, alo);
+                __syncwarp();
+                if (lane < dc.count) {
+                    const uint32_t* cw = sw + c * dc.stride;
+                    long long alo = 0, ahi = 0;
+                    switch (dc.width) {
+                        case 4: column_chunk<4>(cw, dc.count, lane, sX, alo, ahi); break;
+                        case 8: column_chunk<8>(cw, dc.count, lane, sX, alo, ahi); break;
+                        case 12: column_chunk<12>(cw, dc.count, lane, sX, alo, ahi); break;
+                        case 16: column_chunk<16>(cw, dc.count, lane, sX, alo, ahi); break;
+                        case 24: column_chunk<24>(cw, dc.count, lane, sX, alo, ahi); break;
+                        case 32: column_chunk<32>(cw, dc.count, lane, sX, alo, ahi); break;
+                        default: {
+                            long long a2[2];
+                            column_chunk_any(cw, dc.width, dc.count, lane, sX, a2);
+                            alo = a2[0];
+                            ahi = a2[1];
+                        }
+                    }
+                    acc += widen(ahi, alo);
+                }
+                __syncwarp();
             }
-            __syncwarp();
-            if (++cc == dc.nchunks) {
+            ++computed;
+            cc += nc;
+            if (cc == dc.nchunks) {
                 // finished (unit ck, column cp)
                 if (dc.nparts == 1) {
                     if (lane < dc.count) {
@@ -439,22 +453,11 @@ __global__ void __launch_bounds__(kWarps * 32, 2) column_kernel(Arena A, Work W,
                 }
                 xe = W.xe[cp];
             }
+            __syncwarp();
         }
         cp_wait<0>();
         __syncwarp();
     }
-}
-
-// Lanes whose first row lies past the tile read nothing.
-template <int WID>
-__device__ __forceinline__ void row_component(const uint32_t* piece, int lane, bool active, int ul, int uh,
-                                              long long& alo0, long long& ahi0, long long& alo1, long long& ahi1) {
-    int c0 = 0, c1 = 0;
-    if (active) row_pair_codes<WID>(piece, lane, c0, c1);
-    alo0 += (long long)c0 * ul;
-    ahi0 += (long long)c0 * uh;
-    alo1 += (long long)c1 * ul;
-    ahi1 += (long long)c1 * uh;
 }
 
 // acc (on exponent e_acc, kGuard guard bits) += v (on exponent ev); the
@@ -499,20 +502,20 @@ struct RowDesc {
 __global__ void __launch_bounds__(kWarps * 32, 2) row_kernel(Arena A, Work W, double* __restrict__ y,
                                                              int n, int rhs, int n_comp) {
     extern __shared__ __align__(16) uint8_t smem_raw[];
-    __shared__ __int128 s_acc[kWarps][kTileRows];
     __shared__ int s_e[kWarps];
-    __shared__ double s_diag[kTileRows];
-    __shared__ int s_has_diag;
+    __shared__ double s_diag[kDenseSlices][kTileRows];
+    __shared__ int s_nslices;
+    __shared__ __align__(16) int4 s_tab[kWarps][32];
     const RowTile T = A.tiles[blockIdx.x];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    Stage* st = reinterpret_cast<Stage*>(smem_raw) + warp * kStages;
+    uint8_t* slots = smem_raw + (size_t)warp * kStages * kSlotBytes;
     const int r0 = 2 * lane, r1 = 2 * lane + 1;
     const int nunits = T.item1 - T.item0;
     const int my = warp < nunits ? (nunits - warp + kWarps - 1) / kWarps : 0;
-    if (threadIdx.x == 0) s_has_diag = 0;
+    if (threadIdx.x == 0) s_nslices = 0;
     __syncthreads();
-    // All of a warp's units, one per lane, in batches of 32 (units of one
-    // tile rarely exceed 32 per warp).
+    // A warp's units, one descriptor per lane, in batches of 32; pipeline
+    // steps carry as many consecutive units as fit a slot.
     for (int p = 0; p < rhs; ++p) {
         __int128 acc0 = 0, acc1 = 0;
         int e_acc = 0;
@@ -533,94 +536,154 @@ __global__ void __launch_bounds__(kWarps * 32, 2) row_kernel(Arena A, Work W, do
                 d.off = __shfl_sync(0xFFFFFFFFu, mine.off, k);
                 return d;
             };
-            auto issue = [&](int k) {
-                if (k < nb) {
-                    const RowDesc d = desc(k);
-                    if (d.block >= 0) {
-                        Stage& S = st[k % kStages];
-                        const uint32_t* src = A.pwords + d.off;
-                        for (int i = lane; i < (d.words >> 2); i += 32) cp_async16(S.words + 4 * i, src + 4 * i);
-                        if (lane < d.count) cp_async8(&S.v[lane], W.u + (long long)p * n_comp + d.comp + lane);
-                    }
+            // bytes a unit occupies in a slot (words, then its u values)
+            const int my_bytes = (lane < nb && mine.block >= 0) ? mine.words * 4 + ((mine.count * 8 + 15) & ~15) : 0;
+            auto group = [&](int k) {  // units [k, k + m) of one step
+                int m = 1, tot = __shfl_sync(0xFFFFFFFFu, my_bytes, k);
+                while (k + m < nb) {
+                    const int b = __shfl_sync(0xFFFFFFFFu, my_bytes, k + m);
+                    if (tot + b > kSlotBytes) break;
+                    tot += b;
+                    ++m;
                 }
+                return m;
+            };
+            int ik = 0, issued = 0;
+            auto issue = [&]() {
+                if (ik < nb) {
+                    const int m = group(ik);
+                    uint8_t* slot = slots + (issued % kStages) * kSlotBytes;
+                    int off = 0;
+                    for (int q = 0; q < m; ++q) {
+                        const RowDesc d = desc(ik + q);
+                        if (d.block < 0) continue;
+                        uint32_t* sw = reinterpret_cast<uint32_t*>(slot + off);
+                        const uint32_t* src = A.pwords + d.off;
+                        for (int i = lane; i < (d.words >> 2); i += 32) cp_async16(sw + 4 * i, src + 4 * i);
+                        double* sv = reinterpret_cast<double*>(slot + off + d.words * 4);
+                        if (lane < d.count) cp_async8(sv + lane, W.u + (long long)p * n_comp + d.comp + lane);
+                        off += d.words * 4 + ((d.count * 8 + 15) & ~15);
+                    }
+                    ik += m;
+                }
+                ++issued;
                 cp_commit();
             };
 #pragma unroll 1
-            for (int s = 0; s < kStages - 1; ++s) issue(s);
-            for (int k = 0; k < nb; ++k) {
-                issue(k + kStages - 1);
+            for (int s = 0; s < kStages - 1; ++s) issue();
+            int k = 0, computed = 0;
+            while (k < nb) {
+                issue();
                 cp_wait<kStages - 1>();
                 __syncwarp();
-                const RowDesc d = desc(k);
-                const Stage& S = st[k % kStages];
-                if (d.block >= 0) {
-                    // widths from the header, u from the stage
-                    int wl = 0;
-                    double uv = 0.0;
-                    if (lane < d.count) {
-                        wl = int((S.words[lane >> 2] >> (8 * (lane & 3))) & 0xFFu);
-                        uv = S.v[lane];
-                    }
-                    const int eb = __reduce_max_sync(0xFFFFFFFFu, lane < d.count ? exp_field(uv) : 0);
-                    if (eb) {
-                        const long long U = lane < d.count ? to_fixed(uv, eb) : 0;
-                        const int ul_l = int(U & kLimbMask), uh_l = int(U >> kLimb);
-                        const int sz = (T.rows * wl + 31) >> 5;
-                        int incl = sz;
-#pragma unroll
-                        for (int o = 1; o < 32; o <<= 1) {
-                            const int v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-                            if (lane >= o) incl += v;
+                const int m = group(k);
+                const uint8_t* slot = slots + (computed % kStages) * kSlotBytes;
+                int off = 0;
+                for (int q = 0; q < m; ++q) {
+                    const RowDesc d = desc(k + q);
+                    if (d.block >= 0) {
+                        const uint32_t* SW = reinterpret_cast<const uint32_t*>(slot + off);
+                        const double* SV = reinterpret_cast<const double*>(slot + off + d.words * 4);
+                        off += d.words * 4 + ((d.count * 8 + 15) & ~15);
+                        // widths from the header, u from the slot
+                        int wl = 0;
+                        double uv = 0.0;
+                        if (lane < d.count) {
+                            wl = int((SW[lane >> 2] >> (8 * (lane & 3))) & 0xFFu);
+                            uv = SV[lane];
                         }
-                        const int offl = kRowHeaderWords + incl - sz;
-                        long long alo0 = 0, ahi0 = 0, alo1 = 0, ahi1 = 0;
-                        const bool act = r0 < T.rows;
-                        for (int jj = 0; jj < d.count; ++jj) {
-                            const int w = __shfl_sync(0xFFFFFFFFu, wl, jj);
-                            const int ul = __shfl_sync(0xFFFFFFFFu, ul_l, jj);
-                            const int uh = __shfl_sync(0xFFFFFFFFu, uh_l, jj);
-                            const uint32_t* piece = S.words + __shfl_sync(0xFFFFFFFFu, offl, jj);
-                            switch (w) {
-#define QH_ROW_CASE(WW) \
-    case WW:            \
-        row_component<WW>(piece, lane, act, ul, uh, alo0, ahi0, alo1, ahi1); \
-        break;
-                                QH_WIDTH_CASES(QH_ROW_CASE)
-#undef QH_ROW_CASE
-                                default:
-                                    break;
+                        const int eb = __reduce_max_sync(0xFFFFFFFFu, lane < d.count ? exp_field(uv) : 0);
+                        if (eb) {
+                            const long long U = lane < d.count ? to_fixed(uv, eb) : 0;
+                            const int sz = (T.rows * wl + 31) >> 5;
+                            int incl = sz;
+#pragma unroll
+                            for (int o = 1; o < 32; o <<= 1) {
+                                const int v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+                                if (lane >= o) incl += v;
+                            }
+                            int4* tab = s_tab[warp];
+                            tab[lane] = make_int4(int(U & kLimbMask), int(U >> kLimb), kRowHeaderWords + incl - sz, wl);
+                            __syncwarp();
+                            long long alo0 = 0, ahi0 = 0, alo1 = 0, ahi1 = 0;
+                            long long blo0 = 0, bhi0 = 0, blo1 = 0, bhi1 = 0;
+                            if (r0 < T.rows) {
+                                int j = 0;
+                                for (; j + 1 < d.count; j += 2) {
+                                    const int4 t0 = tab[j], t1 = tab[j + 1];
+                                    int c0, c1, e0, e1;
+                                    row_pair_codes_rt(SW + t0.z, lane, t0.w, c0, c1);
+                                    row_pair_codes_rt(SW + t1.z, lane, t1.w, e0, e1);
+                                    alo0 += (long long)c0 * t0.x;
+                                    ahi0 += (long long)c0 * t0.y;
+                                    alo1 += (long long)c1 * t0.x;
+                                    ahi1 += (long long)c1 * t0.y;
+                                    blo0 += (long long)e0 * t1.x;
+                                    bhi0 += (long long)e0 * t1.y;
+                                    blo1 += (long long)e1 * t1.x;
+                                    bhi1 += (long long)e1 * t1.y;
+                                }
+                                if (j < d.count) {
+                                    const int4 t0 = tab[j];
+                                    int c0, c1;
+                                    row_pair_codes_rt(SW + t0.z, lane, t0.w, c0, c1);
+                                    alo0 += (long long)c0 * t0.x;
+                                    ahi0 += (long long)c0 * t0.y;
+                                    alo1 += (long long)c1 * t0.x;
+                                    ahi1 += (long long)c1 * t0.y;
+                                }
+                            }
+                            alo0 += blo0;
+                            ahi0 += bhi0;
+                            alo1 += blo1;
+                            ahi1 += bhi1;
+                            __syncwarp();
+                            __int128 v0 = widen(ahi0, alo0), v1 = widen(ahi1, alo1);
+                            if (r0 >= T.rows) v0 = 0;
+                            if (r1 >= T.rows) v1 = 0;
+                            add_aligned(acc0, acc1, e_acc, v0, v1, eb);
+                        }
+                    } else {
+                        // column slice of a dense diagonal block (column-major values)
+                        const DenseDesc dd = A.dd[-1 - d.block];
+                        const double* D = A.dense + d.off;
+                        const double* xcp = W.xc + (long long)p * n + dd.col0 + d.words;
+                        double dg0 = 0.0, dg1 = 0.0;
+                        const bool v0 = r0 < T.rows, v1 = r1 < T.rows;
+                        // eight columns at a time: all loads issued before the FMA chain
+                        for (int k0 = 0; k0 < d.count; k0 += 8) {
+                            double xv[8], a0v[8], a1v[8];
+#pragma unroll
+                            for (int q = 0; q < 8; ++q) {
+                                const int kk = k0 + q;
+                                const bool in = kk < d.count;
+                                const double* col = D + (long long)kk * dd.m;
+                                xv[q] = in ? __ldg(xcp + kk) : 0.0;
+                                a0v[q] = (in && v0) ? __ldg(col + r0) : 0.0;
+                                a1v[q] = (in && v1) ? __ldg(col + r1) : 0.0;
+                            }
+#pragma unroll
+                            for (int q = 0; q < 8; ++q) {
+                                dg0 = fma(a0v[q], xv[q], dg0);
+                                dg1 = fma(a1v[q], xv[q], dg1);
                             }
                         }
-                        __int128 v0 = widen(ahi0, alo0), v1 = widen(ahi1, alo1);
-                        if (r0 >= T.rows) v0 = 0;
-                        if (r1 >= T.rows) v1 = 0;
-                        add_aligned(acc0, acc1, e_acc, v0, v1, eb);
+                        s_diag[d.comp][r0] = dg0;
+                        s_diag[d.comp][r1] = dg1;
+                        if (lane == 0) atomicMax(&s_nslices, d.comp + 1);
                     }
-                } else {
-                    // dense diagonal block (at most one per tile), column-major values
-                    const DenseDesc dd = A.dd[-1 - d.block];
-                    const double* D = A.dense + d.off;
-                    const double* xcp = W.xc + (long long)p * n + dd.col0;
-                    double dg0 = 0.0, dg1 = 0.0;
-                    const bool v0 = r0 < T.rows, v1 = r1 < T.rows;
-#pragma unroll 4
-                    for (int kk = 0; kk < dd.n; ++kk) {
-                        const double xk = __ldg(xcp + kk);
-                        const double* col = D + (long long)kk * dd.m;
-                        if (v0) dg0 = fma(__ldg(col + r0), xk, dg0);
-                        if (v1) dg1 = fma(__ldg(col + r1), xk, dg1);
-                    }
-                    s_diag[r0] = dg0;
-                    s_diag[r1] = dg1;
-                    s_has_diag = 1;
                 }
+                k += m;
+                ++computed;
                 __syncwarp();
             }
             cp_wait<0>();
             __syncwarp();
         }
-        s_acc[warp][r0] = acc0;
-        s_acc[warp][r1] = acc1;
+        // row sums go to the warp's own (drained) stage 0 for the combine
+        __int128* wacc = reinterpret_cast<__int128*>(slots);
+        wacc[r0] = acc0;
+        wacc[r1] = acc1;
         if (lane == 0) s_e[warp] = e_acc;
         __syncthreads();
         if (threadIdx.x < T.rows) {
@@ -632,12 +695,13 @@ __global__ void __launch_bounds__(kWarps * 32, 2) row_kernel(Arena A, Work W, do
 #pragma unroll
             for (int i = 0; i < kWarps; ++i) {
                 const int dsh = et - s_e[i];
-                const __int128 a = s_acc[i][r];
+                const __int128 a = reinterpret_cast<const __int128*>(smem_raw + (size_t)i * kStages * kSlotBytes)[r];
                 if (dsh == 0) tot += a;
                 else if (dsh < 127) tot += (a + ((__int128)1 << (dsh - 1))) >> dsh;
             }
             const double lr = et ? scalbn(i128_to_double(tot), et - 1022 - kFixBits - kGuard) : 0.0;
-            const double dg = s_has_diag ? s_diag[r] : 0.0;
+            double dg = 0.0;
+            for (int sl = 0; sl < s_nslices; ++sl) dg += s_diag[sl][r];
             y[(long long)__ldg(A.perm + T.row0 + r) * rhs + p] = dg + lr;
         }
         __syncthreads();
@@ -695,16 +759,7 @@ __global__ void decode_row_kernel(Arena A, int n_tiles, const long long* __restr
             for (int j = 0; j < I.count; ++j) {
                 const int w = int((blk[j >> 2] >> (8 * (j & 3))) & 0xFFu);
                 int c0 = 0, c1 = 0;
-                switch (2 * lane < T.rows ? w : 0) {
-#define QH_DEC_CASE(WW)                                \
-    case WW:                                           \
-        row_pair_codes<WW>(piece, lane, c0, c1);       \
-        break;
-                    QH_WIDTH_CASES(QH_DEC_CASE)
-#undef QH_DEC_CASE
-                    default:
-                        break;
-                }
+                if (2 * lane < T.rows) row_pair_codes_rt(piece, lane, w, c0, c1);
                 const long long o = comp_off[I.comp + j] + I.rloc0;
                 if (2 * lane < T.rows) out[o + 2 * lane] = c0;
                 if (2 * lane + 1 < T.rows) out[o + 2 * lane + 1] = c1;
