@@ -128,6 +128,28 @@ QH_API int qh_matmul_device_profiled(const qh_matrix* m, const double* x, double
                                      void* workspace, size_t workspace_bytes, void* stream,
                                      int* status, void* const* events4);
 
+/* Bytes of the fixed device scratch array qh_matmul_device_static uses. */
+#define QH_STATIC_SCRATCH_BYTES (16u << 20)
+
+/* qh_matmul_device for callers that cannot allocate device memory during an
+ * apply -- a plugin whose host framework owns all device memory through its
+ * own allocator, a latency-critical loop that cannot afford cudaMalloc's
+ * implicit device synchronisation, code held to a fixed pre-reserved memory
+ * budget.  It allocates nothing: its scratch is a file-scope static
+ * __device__ array of QH_STATIC_SCRATCH_BYTES (16 MiB) that every GPU which
+ * loads this library holds until the process exits.  The caller still passes
+ * x and y (device pointers, row-major order x rhs, source order), the stream
+ * and the optional status int, as for qh_matmul_device.  An apply whose
+ * scratch (qh_workspace_bytes(m, rhs)) exceeds QH_STATIC_SCRATCH_BYTES is
+ * rejected with QH_EINVAL.  The first call on a device looks up the array's
+ * device address (cudaGetSymbolAddress) and caches it; make that first call
+ * before any stream capture.  All calls share the one array (each call clears
+ * the parts that must start at zero), so calls that overlap on the GPU --
+ * concurrent streams, or several threads -- race and must be serialised by
+ * the caller.  No counterpart in the reference. */
+QH_API int qh_matmul_device_static(const qh_matrix* m, const double* x, double* y, size_t rhs,
+                                   void* stream, int* status);
+
 /* Drop-in for HMatrix::matmul_cuda: host x (order*rhs doubles), host y.
  * Copies x in through pinned staging, applies, copies y back and
  * synchronises.  Raises the reference's errors: "right-hand-side shape

@@ -66,6 +66,8 @@ def load_library() -> C.CDLL:
     lib.qh_matmul_device.argtypes = [vp, vp, vp, sz, vp, sz, vp, vp]
     lib.qh_matmul_device_profiled.restype = i32
     lib.qh_matmul_device_profiled.argtypes = [vp, vp, vp, sz, vp, sz, vp, vp, vp]
+    lib.qh_matmul_device_static.restype = i32
+    lib.qh_matmul_device_static.argtypes = [vp, vp, vp, sz, vp, vp]
     lib.qh_matmul_host.restype = i32
     lib.qh_matmul_host.argtypes = [vp, vp, vp, sz]
     lib.qh_fnv1a64.restype = C.c_uint64

@@ -789,6 +789,12 @@ size_t align256(size_t v) { return (v + 255) & ~size_t(255); }
 
 using namespace qhg;
 
+// Scratch of qh_matmul_device_static: one fixed array per device, loaded with
+// the library and held until exit.  Host code must not use this symbol as an
+// address (it names a host-side stand-in); static_scratch() returns the
+// device address for the current device.
+static __device__ __align__(256) unsigned char g_static_scratch[QH_STATIC_SCRATCH_BYTES];
+
 struct qh_matrix {
     Layout L;
     int device = 0;
@@ -1099,6 +1105,38 @@ int qh_matmul_device_profiled(const qh_matrix* m, const double* x, double* y, si
         mm->own_ws_bytes = need;
     }
     return launch(m, x, y, rhs, mm->own_ws, static_cast<cudaStream_t>(stream), status, events4);
+}
+
+int qh_matmul_device_static(const qh_matrix* m, const double* x, double* y, size_t rhs, void* stream,
+                            int* status) {
+    if (!m) return fail(QH_EINVAL, "null matrix handle");
+    int rc = check_rhs(m, rhs);
+    if (rc) return rc;
+    if (!x || !y) return fail(QH_EINVAL, "null right-hand side or result pointer");
+    const size_t need = ws_bytes(m->L, rhs);
+    if (need > size_t(QH_STATIC_SCRATCH_BYTES))
+        return fail(QH_EINVAL, "qh_matmul_device_static: this apply needs " + std::to_string(need) +
+                                   " bytes of scratch, more than the fixed " +
+                                   std::to_string(size_t(QH_STATIC_SCRATCH_BYTES)) +
+                                   " (QH_STATIC_SCRATCH_BYTES); use qh_matmul_device with a workspace");
+    DeviceGuard g(m->device);
+    // Device address of the array, looked up once per device with that device
+    // current (the first call on a device does this set-up).
+    static std::mutex mu;
+    static void* addr[64] = {nullptr};
+    if (m->device < 0 || m->device >= 64) return fail(QH_EINVAL, "invalid CUDA device ordinal");
+    void* ptr = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        if (!addr[m->device]) {
+            void* p = nullptr;
+            cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+            if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress");
+            addr[m->device] = p;
+        }
+        ptr = addr[m->device];
+    }
+    return launch(m, x, y, rhs, ptr, static_cast<cudaStream_t>(stream), status);
 }
 
 int qh_matmul_host(const qh_matrix* m, const double* x, double* y, size_t rhs) {
