@@ -107,11 +107,6 @@ __device__ __forceinline__ __int128 widen(long long hi, long long lo) {
     return ((__int128)hi << kLimb) + lo;
 }
 
-__device__ __forceinline__ double i128_to_double(__int128 v) {
-    const long long hi = (long long)(v >> 64);
-    const unsigned long long lo = (unsigned long long)v;
-    return fma(double(hi), 18446744073709551616.0, double(lo));
-}
 
 struct Arena {
     const int32_t* perm;
@@ -136,31 +131,100 @@ struct Work {
     double* u;         // [rhs][n_comp] u_bj = s^P s^Q t_bj (FP64)
 };
 
-// ------------------------------------------------------------ cp.async
+// -------------------------------------------------- bulk copies (TMA)
 
-__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
-    const unsigned s = unsigned(__cvta_generic_to_shared(smem));
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return unsigned(__cvta_generic_to_shared(p)); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count) : "memory");
 }
-__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
-    const unsigned s = unsigned(__cvta_generic_to_shared(smem));
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+__device__ __forceinline__ void mbar_init_fence() {
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
 }
-__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_wait() {
-    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+// Arrive once and expect `bytes` more bytes of transactions on this phase.
+__device__ __forceinline__ void mbar_arrive_expect(uint64_t* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait: gives up (returns false) after kWaitLimit polls instead of
+// hanging; callers record the failure in the status word and stop.
+constexpr int kWaitLimit = 1 << 22;
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
+    for (int i = 0; i < kWaitLimit; ++i)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+// Order this thread's (and, after a warp barrier, its warp's) earlier generic
+// accesses to shared memory before later asynchronous-proxy writes to it.
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+// One-dimensional bulk copy global -> shared (16-byte aligned, bytes % 16 == 0),
+// completing on `bar`.
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
 }
 
-// One stage of a warp's prefetch pipeline: code words plus 32 doubles (x
-// entries on the column side, u values on the row side).
-struct Stage {
-    uint32_t words[kStageWordBytes / 4];
-    double v[32];
-};
+// Slot of a warp's prefetch pipeline: up to 4 KB of code words plus up to 33
+// doubles (x entries or u values, copied from an 8-byte-aligned start rounded
+// down to 16 bytes).
+constexpr int kSlotBytes = kStageWordBytes + 272;
 constexpr int kStages = 3;
 constexpr int kWarps = 8;
-constexpr int kPipeSmem = kWarps * kStages * int(sizeof(Stage));
+constexpr int kPipeSmem = kWarps * kStages * kSlotBytes;
+
+// Status bits written by the kernels (status word of the apply).
+constexpr int kStatusNonfinite = 1;
+constexpr int kStatusTimeout = 2;
+
+__device__ __forceinline__ void flag_timeout(int* status) {
+    if (status) atomicOr(status, kStatusTimeout);
+}
+
+// round(v * 2^k) for a 128-bit integer v, as a double, with integer
+// operations only (round to nearest even; results outside the normal range
+// take the slow path).
+__device__ __forceinline__ double i128_ldexp(__int128 v, int k) {
+    if (v == 0) return 0.0;
+    const bool neg = v < 0;
+    const unsigned __int128 a = neg ? (unsigned __int128)(-v) : (unsigned __int128)v;
+    const unsigned long long hi = (unsigned long long)(a >> 64), lo = (unsigned long long)a;
+    const int nbits = hi ? 128 - __clzll(hi) : 64 - __clzll(lo);
+    unsigned long long mant;
+    int e;
+    if (nbits <= 53) {
+        mant = lo << (53 - nbits);
+        e = nbits - 53;
+    } else {
+        const int sh = nbits - 53;
+        const unsigned __int128 q = a >> sh;
+        const unsigned __int128 rem = a - (q << sh);
+        const unsigned __int128 half = (unsigned __int128)1 << (sh - 1);
+        mant = (unsigned long long)q;
+        if (rem > half || (rem == half && (mant & 1))) ++mant;
+        e = sh;
+        if (mant >> 53) {
+            mant >>= 1;
+            ++e;
+        }
+    }
+    const int E = e + k + 52 + 1023;
+    if (E <= 0 || E >= 2047) return scalbn(neg ? -double(mant) : double(mant), e + k);
+    const unsigned long long bits =
+        ((unsigned long long)neg << 63) | ((unsigned long long)E << 52) | (mant & 0xFFFFFFFFFFFFFULL);
+    return __longlong_as_double((long long)bits);
+}
 
 // ------------------------------------------------------------- decoders
 
@@ -216,7 +280,7 @@ __global__ void __launch_bounds__(256) prep_x_kernel(Arena A, Work W, const doub
     const bool valid = pos < n;
     const double v = valid ? __ldg(x + (long long)__ldg(A.perm + pos) * rhs + p) : 0.0;
     const int e = exp_field(v);
-    if (__any_sync(0xFFFFFFFFu, e == 0x7FF) && lane == 0 && status) *status = 1;
+    if (__any_sync(0xFFFFFFFFu, e == 0x7FF) && lane == 0 && status) atomicOr(status, kStatusNonfinite);
     const int emax = __reduce_max_sync(0xFFFFFFFFu, e == 0x7FF ? 0 : e);
     if (valid) W.xc[(long long)p * n + pos] = e == 0x7FF ? 0.0 : v;
     if (lane == 0 && emax) atomicMax(W.xe + p, emax);
@@ -304,33 +368,40 @@ __device__ __forceinline__ ColDesc shfl_desc(const ColDesc& d, int src) {
     return r;
 }
 
-constexpr int kSlotBytes = int(sizeof(Stage));
-
 // Chunks of one (unit, column) that one pipeline step carries: as many as fit
 // a slot (code words plus 32 x entries per chunk), at least one.
 __device__ __forceinline__ int col_step_chunks(int stride, int remaining) {
     const int per = stride * 4 + kColChunk * 8;
-    return max(1, min(remaining, kSlotBytes / per));
+    return max(1, min(remaining, (kSlotBytes - 16) / per));
 }
 
 // Column side.  Warp gw owns units gw, gw + G, ... (heaviest first); its work
 // is the sequence (unit, rhs column, chunk), streamed through a kStages-deep
-// cp.async pipeline whose steps carry as many chunks as fit a slot: chunk
-// words and the chunks' x entries are copied to shared memory kStages - 1
-// steps ahead of their use.  Lane l accumulates component l of the unit
-// exactly; a unit's last chunk converts the sum (or, for a split task, hands
-// it to the part that finishes last).
+// pipeline of shared-memory slots filled by bulk copies (one per step for the
+// code words, one for the x entries), kStages - 1 steps ahead of their use;
+// a step carries as many chunks as fit a slot.  Lane l accumulates component
+// l of the unit exactly; a unit's last chunk converts the sum (or, for a
+// split task, hands it to the part that finishes last).
 __global__ void __launch_bounds__(kWarps * 32, 2) column_kernel(Arena A, Work W, int n_tasks, int n, int rhs,
-                                                                int n_comp, int max_parts) {
+                                                                int n_comp, int max_parts, int* status) {
     extern __shared__ __align__(16) uint8_t smem_raw[];
     __shared__ __align__(16) int2 sXall[kWarps][kColChunk];
+    __shared__ __align__(8) uint64_t s_bar[kWarps][kStages];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint8_t* slots = smem_raw + (size_t)warp * kStages * kSlotBytes;
+    uint64_t* bar = s_bar[warp];
     int2* sX = sXall[warp];
+    if (lane == 0) {
+        for (int i = 0; i < kStages; ++i) mbar_init(bar + i, 1);
+        mbar_init_fence();
+    }
+    __syncwarp();
     const int G = gridDim.x * kWarps;
     const int gw = blockIdx.x * kWarps + warp;
     const int my_units = gw < n_tasks ? (n_tasks - gw + G - 1) / G : 0;
-    for (int b0 = 0; b0 < my_units; b0 += 32) {
+    unsigned issued = 0, computed = 0;  // running step counters (slot, phase)
+    bool failed = false;
+    for (int b0 = 0; b0 < my_units && !failed; b0 += 32) {
         const int nb = min(32, my_units - b0);
         ColDesc mine{};
         if (lane < nb) {
@@ -338,47 +409,59 @@ __global__ void __launch_bounds__(kWarps * 32, 2) column_kernel(Arena A, Work W,
             mine = {T.word0, T.col0, T.n, T.width, T.count, T.stride, T.comp_idx, T.chunk0, T.nchunks,
                     T.part, T.nparts, T.split_id};
         }
-        int ik = 0, ip = 0, ic = 0, issued = 0;  // issue cursor
+        int ik = 0, ip = 0, ic = 0;  // issue cursor
         ColDesc di = shfl_desc(mine, 0);
         auto issue = [&]() {
-            if (ik < nb) {
-                const int nc = col_step_chunks(di.stride, di.nchunks - ic);
-                uint8_t* slot = slots + (issued % kStages) * kSlotBytes;
-                uint32_t* sw = reinterpret_cast<uint32_t*>(slot);
-                double* sv = reinterpret_cast<double*>(slot + nc * di.stride * 4);
-                const uint32_t* src = A.qwords + di.word0 + (long long)(di.chunk0 + ic) * di.stride;
-                const int n16 = (nc * di.stride) >> 2;
-                for (int i = lane; i < n16; i += 32) cp_async16(sw + 4 * i, src + 4 * i);
-                for (int c = 0; c < nc; ++c) {
-                    const int k = (di.chunk0 + ic + c) * kColChunk + lane;
-                    if (k < di.n) cp_async8(sv + c * kColChunk + lane, W.xc + (long long)ip * n + di.col0 + k);
-                }
-                ic += nc;
-                if (ic == di.nchunks) {
-                    ic = 0;
-                    if (++ip == rhs) {
-                        ip = 0;
-                        if (++ik < nb) di = shfl_desc(mine, ik);
-                    }
-                }
+            if (ik >= nb) return;
+            const int nc = col_step_chunks(di.stride, di.nchunks - ic);
+            const unsigned slot_i = issued % kStages;
+            uint8_t* slot = slots + slot_i * kSlotBytes;
+            const unsigned wbytes = unsigned(nc * di.stride * 4);
+            const int k0 = (di.chunk0 + ic) * kColChunk;
+            const int cnt = min(di.n - k0, nc * kColChunk);
+            const double* xa = W.xc + (long long)ip * n + di.col0 + k0;
+            const int xs = int((reinterpret_cast<uintptr_t>(xa) >> 3) & 1);
+            const unsigned xbytes = unsigned(((cnt + xs) * 8 + 15) & ~15);
+            if (lane == 0) {
+                fence_async_smem();
+                mbar_arrive_expect(bar + slot_i, wbytes + xbytes);
+                bulk_load(slot, A.qwords + di.word0 + (long long)(di.chunk0 + ic) * di.stride, wbytes, bar + slot_i);
+                bulk_load(slot + wbytes, xa - xs, xbytes, bar + slot_i);
             }
             ++issued;
-            cp_commit();
+            ic += nc;
+            if (ic == di.nchunks) {
+                ic = 0;
+                if (++ip == rhs) {
+                    ip = 0;
+                    if (++ik < nb) di = shfl_desc(mine, ik);
+                }
+            }
         };
+        __syncwarp();
 #pragma unroll 1
         for (int s = 0; s < kStages - 1; ++s) issue();
-        int ck = 0, cp = 0, cc = 0, computed = 0;  // compute cursor
+        int ck = 0, cp = 0, cc = 0;  // compute cursor
         ColDesc dc = shfl_desc(mine, 0);
         __int128 acc = 0;
         int xe = W.xe[0];
+        // finalize operands, loaded as soon as a unit starts
+        int comp_id = lane < dc.count ? __ldg(A.task_comp + dc.comp_idx + lane) : 0;
+        double comp_sc = lane < dc.count ? __ldg(A.comp_s + comp_id) : 0.0;
         while (ck < nb) {
             issue();
-            cp_wait<kStages - 1>();
-            __syncwarp();
+            const unsigned slot_i = computed % kStages;
+            if (!mbar_wait(bar + slot_i, (computed / kStages) & 1)) {
+                flag_timeout(status);
+                failed = true;
+                break;
+            }
             const int nc = col_step_chunks(dc.stride, dc.nchunks - cc);
-            const uint8_t* slot = slots + (computed % kStages) * kSlotBytes;
+            const uint8_t* slot = slots + slot_i * kSlotBytes;
             const uint32_t* sw = reinterpret_cast<const uint32_t*>(slot);
-            const double* sv = reinterpret_cast<const double*>(slot + nc * dc.stride * 4);
+            const double* xa = W.xc + (long long)cp * n + dc.col0 + (dc.chunk0 + cc) * kColChunk;
+            const int xs = int((reinterpret_cast<uintptr_t>(xa) >> 3) & 1);
+            const double* sv = reinterpret_cast<const double*>(slot + nc * dc.stride * 4) + xs;
             for (int c = 0; c < nc; ++c) {
                 // the chunk's x entries on the column's exponent, as limbs
                 {
@@ -412,13 +495,10 @@ __global__ void __launch_bounds__(kWarps * 32, 2) column_kernel(Arena A, Work W,
             ++computed;
             cc += nc;
             if (cc == dc.nchunks) {
-                // finished (unit ck, column cp)
+                // finished (unit ck, column cp); x ~= X * 2^(xe - 1022 - kFixBits)
                 if (dc.nparts == 1) {
-                    if (lane < dc.count) {
-                        const int c = __ldg(A.task_comp + dc.comp_idx + lane);
-                        const double t = xe ? scalbn(i128_to_double(acc), xe - 1022 - kFixBits) : 0.0;
-                        W.u[(long long)cp * n_comp + c] = t * __ldg(A.comp_s + c);
-                    }
+                    if (lane < dc.count)
+                        W.u[(long long)cp * n_comp + comp_id] = xe ? i128_ldexp(acc, xe - 1022 - kFixBits) * comp_sc : 0.0;
                 } else {
                     long long* part = W.part + (((long long)dc.split_id * max_parts + dc.part) * rhs + cp) * 64;
                     part[2 * lane] = (long long)acc;
@@ -438,25 +518,30 @@ __global__ void __launch_bounds__(kWarps * 32, 2) column_kernel(Arena A, Work W,
                             const long long hi = __ldcg(pq + 2 * lane + 1);
                             tot += ((__int128)hi << 64) | lo;
                         }
-                        if (lane < dc.count) {
-                            const int c = __ldg(A.task_comp + dc.comp_idx + lane);
-                            const double t = xe ? scalbn(i128_to_double(tot), xe - 1022 - kFixBits) : 0.0;
-                            W.u[(long long)cp * n_comp + c] = t * __ldg(A.comp_s + c);
-                        }
+                        if (lane < dc.count)
+                            W.u[(long long)cp * n_comp + comp_id] =
+                                xe ? i128_ldexp(tot, xe - 1022 - kFixBits) * comp_sc : 0.0;
                     }
                 }
                 acc = 0;
                 cc = 0;
                 if (++cp == rhs) {
                     cp = 0;
-                    if (++ck < nb) dc = shfl_desc(mine, ck);
+                    if (++ck < nb) {
+                        dc = shfl_desc(mine, ck);
+                        comp_id = lane < dc.count ? __ldg(A.task_comp + dc.comp_idx + lane) : 0;
+                        comp_sc = lane < dc.count ? __ldg(A.comp_s + comp_id) : 0.0;
+                    }
                 }
                 xe = W.xe[cp];
             }
             __syncwarp();
         }
-        cp_wait<0>();
-        __syncwarp();
+    }
+    // copies still in flight (only after a failed wait): wait for them, bounded
+    while (computed < issued) {
+        mbar_wait(bar + computed % kStages, (computed / kStages) & 1);
+        ++computed;
     }
 }
 
@@ -500,8 +585,9 @@ struct RowDesc {
 // with kGuard guard bits.  Dense diagonal units use FP64 loads directly.
 // Warps combine per rhs column in shared memory in a fixed order.
 __global__ void __launch_bounds__(kWarps * 32, 2) row_kernel(Arena A, Work W, double* __restrict__ y,
-                                                             int n, int rhs, int n_comp) {
+                                                             int n, int rhs, int n_comp, int* status) {
     extern __shared__ __align__(16) uint8_t smem_raw[];
+    __shared__ __align__(8) uint64_t s_bar[kWarps][kStages];
     __shared__ int s_e[kWarps];
     __shared__ double s_diag[kDenseSlices][kTileRows];
     __shared__ int s_nslices;
@@ -509,17 +595,24 @@ __global__ void __launch_bounds__(kWarps * 32, 2) row_kernel(Arena A, Work W, do
     const RowTile T = A.tiles[blockIdx.x];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint8_t* slots = smem_raw + (size_t)warp * kStages * kSlotBytes;
+    uint64_t* bar = s_bar[warp];
     const int r0 = 2 * lane, r1 = 2 * lane + 1;
     const int nunits = T.item1 - T.item0;
     const int my = warp < nunits ? (nunits - warp + kWarps - 1) / kWarps : 0;
     if (threadIdx.x == 0) s_nslices = 0;
+    if (lane == 0) {
+        for (int i = 0; i < kStages; ++i) mbar_init(bar + i, 1);
+        mbar_init_fence();
+    }
     __syncthreads();
+    unsigned issued = 0, computed = 0;  // running step counters (slot, phase)
+    bool failed = false;
     // A warp's units, one descriptor per lane, in batches of 32; pipeline
     // steps carry as many consecutive units as fit a slot.
     for (int p = 0; p < rhs; ++p) {
         __int128 acc0 = 0, acc1 = 0;
         int e_acc = 0;
-        for (int b0 = 0; b0 < my; b0 += 32) {
+        for (int b0 = 0; b0 < my && !failed; b0 += 32) {
             const int nb = min(32, my - b0);
             RowDesc mine{};
             if (lane < nb) {
@@ -536,8 +629,10 @@ __global__ void __launch_bounds__(kWarps * 32, 2) row_kernel(Arena A, Work W, do
                 d.off = __shfl_sync(0xFFFFFFFFu, mine.off, k);
                 return d;
             };
-            // bytes a unit occupies in a slot (words, then its u values)
-            const int my_bytes = (lane < nb && mine.block >= 0) ? mine.words * 4 + ((mine.count * 8 + 15) & ~15) : 0;
+            // bytes a unit occupies in a slot (words, then its u values copied
+            // from an 8-byte-aligned start rounded down to 16 bytes)
+            const int my_bytes =
+                (lane < nb && mine.block >= 0) ? mine.words * 4 + ((mine.count + 1) * 8 + 15) / 16 * 16 : 0;
             auto group = [&](int k) {  // units [k, k + m) of one step
                 int m = 1, tot = __shfl_sync(0xFFFFFFFFu, my_bytes, k);
                 while (k + m < nb) {
@@ -548,43 +643,58 @@ __global__ void __launch_bounds__(kWarps * 32, 2) row_kernel(Arena A, Work W, do
                 }
                 return m;
             };
-            int ik = 0, issued = 0;
+            int ik = 0;
             auto issue = [&]() {
-                if (ik < nb) {
-                    const int m = group(ik);
-                    uint8_t* slot = slots + (issued % kStages) * kSlotBytes;
-                    int off = 0;
-                    for (int q = 0; q < m; ++q) {
-                        const RowDesc d = desc(ik + q);
-                        if (d.block < 0) continue;
-                        uint32_t* sw = reinterpret_cast<uint32_t*>(slot + off);
-                        const uint32_t* src = A.pwords + d.off;
-                        for (int i = lane; i < (d.words >> 2); i += 32) cp_async16(sw + 4 * i, src + 4 * i);
-                        double* sv = reinterpret_cast<double*>(slot + off + d.words * 4);
-                        if (lane < d.count) cp_async8(sv + lane, W.u + (long long)p * n_comp + d.comp + lane);
-                        off += d.words * 4 + ((d.count * 8 + 15) & ~15);
+                if (ik >= nb) return;
+                const int m = group(ik);
+                const unsigned slot_i = issued % kStages;
+                uint8_t* slot = slots + slot_i * kSlotBytes;
+                // total bytes of the step, then the copies (lane 0)
+                unsigned total = 0;
+                for (int q = 0; q < m; ++q) total += unsigned(__shfl_sync(0xFFFFFFFFu, my_bytes, ik + q));
+                if (lane == 0) {
+                    fence_async_smem();
+                    mbar_arrive_expect(bar + slot_i, total);
+                }
+                int off = 0;
+                for (int q = 0; q < m; ++q) {
+                    const RowDesc d = desc(ik + q);
+                    if (d.block < 0) continue;
+                    const double* ua = W.u + (long long)p * n_comp + d.comp;
+                    const int us = int((reinterpret_cast<uintptr_t>(ua) >> 3) & 1);
+                    const unsigned ubytes = unsigned(((d.count + 1) * 8 + 15) / 16 * 16);
+                    if (lane == 0) {
+                        bulk_load(slot + off, A.pwords + d.off, unsigned(d.words * 4), bar + slot_i);
+                        bulk_load(slot + off + d.words * 4, ua - us, ubytes, bar + slot_i);
                     }
-                    ik += m;
+                    off += d.words * 4 + int(ubytes);
                 }
                 ++issued;
-                cp_commit();
+                ik += m;
             };
+            __syncwarp();
 #pragma unroll 1
             for (int s = 0; s < kStages - 1; ++s) issue();
-            int k = 0, computed = 0;
+            int k = 0;
             while (k < nb) {
                 issue();
-                cp_wait<kStages - 1>();
-                __syncwarp();
+                const unsigned slot_i = computed % kStages;
+                if (!mbar_wait(bar + slot_i, (computed / kStages) & 1)) {
+                    flag_timeout(status);
+                    failed = true;
+                    break;
+                }
                 const int m = group(k);
-                const uint8_t* slot = slots + (computed % kStages) * kSlotBytes;
+                const uint8_t* slot = slots + slot_i * kSlotBytes;
                 int off = 0;
                 for (int q = 0; q < m; ++q) {
                     const RowDesc d = desc(k + q);
                     if (d.block >= 0) {
                         const uint32_t* SW = reinterpret_cast<const uint32_t*>(slot + off);
-                        const double* SV = reinterpret_cast<const double*>(slot + off + d.words * 4);
-                        off += d.words * 4 + ((d.count * 8 + 15) & ~15);
+                        const double* ua = W.u + (long long)p * n_comp + d.comp;
+                        const int us = int((reinterpret_cast<uintptr_t>(ua) >> 3) & 1);
+                        const double* SV = reinterpret_cast<const double*>(slot + off + d.words * 4) + us;
+                        off += d.words * 4 + ((d.count + 1) * 8 + 15) / 16 * 16;
                         // widths from the header, u from the slot
                         int wl = 0;
                         double uv = 0.0;
@@ -677,8 +787,8 @@ __global__ void __launch_bounds__(kWarps * 32, 2) row_kernel(Arena A, Work W, do
                 ++computed;
                 __syncwarp();
             }
-            cp_wait<0>();
-            __syncwarp();
+            // after a failed wait the warp does no more work but still takes
+            // part in the tile's barriers below
         }
         // row sums go to the warp's own (drained) stage 0 for the combine
         __int128* wacc = reinterpret_cast<__int128*>(slots);
@@ -699,12 +809,17 @@ __global__ void __launch_bounds__(kWarps * 32, 2) row_kernel(Arena A, Work W, do
                 if (dsh == 0) tot += a;
                 else if (dsh < 127) tot += (a + ((__int128)1 << (dsh - 1))) >> dsh;
             }
-            const double lr = et ? scalbn(i128_to_double(tot), et - 1022 - kFixBits - kGuard) : 0.0;
+            const double lr = et ? i128_ldexp(tot, et - 1022 - kFixBits - kGuard) : 0.0;
             double dg = 0.0;
             for (int sl = 0; sl < s_nslices; ++sl) dg += s_diag[sl][r];
             y[(long long)__ldg(A.perm + T.row0 + r) * rhs + p] = dg + lr;
         }
         __syncthreads();
+    }
+    // copies still in flight (only after a failed wait): wait for them, bounded
+    while (computed < issued) {
+        mbar_wait(bar + computed % kStages, (computed / kStages) & 1);
+        ++computed;
     }
 }
 
@@ -923,9 +1038,10 @@ WsPlan ws_plan(const Layout& L, size_t rhs) {
     w.xe = take(4 * rhs);
     w.cnt = take(4 * size_t(L.n_split) * rhs);
     w.zero_bytes = off;
-    w.xc = take(8 * L.order * rhs);
+    // xc and u are read by 16-byte-rounded bulk copies: keep 32 spare bytes
+    w.xc = take(8 * L.order * rhs + 32);
     w.part = take(16 * 32 * size_t(L.n_split) * size_t(L.max_parts) * rhs);
-    w.u = take(8 * size_t(L.n_comp) * rhs);
+    w.u = take(8 * size_t(L.n_comp) * rhs + 32);
     w.total = off;
     return w;
 }
@@ -955,10 +1071,11 @@ int launch(const qh_matrix* m, const double* x, double* y, size_t rhs, void* ws,
     mark(1);
     if (L.n_tasks > 0) {
         const int grid = std::max(1, std::min((L.n_tasks + kWarps - 1) / kWarps, m->sms * 2));
-        column_kernel<<<grid, kWarps * 32, kPipeSmem, s>>>(m->A, W, L.n_tasks, n, int(rhs), L.n_comp, L.max_parts);
+        column_kernel<<<grid, kWarps * 32, kPipeSmem, s>>>(m->A, W, L.n_tasks, n, int(rhs), L.n_comp, L.max_parts,
+                                                            status);
     }
     mark(2);
-    row_kernel<<<L.n_tiles, kWarps * 32, kPipeSmem, s>>>(m->A, W, y, n, int(rhs), L.n_comp);
+    row_kernel<<<L.n_tiles, kWarps * 32, kPipeSmem, s>>>(m->A, W, y, n, int(rhs), L.n_comp, status);
     mark(3);
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "CUDA kernel launch");
@@ -1196,7 +1313,8 @@ int qh_matmul_host(const qh_matrix* m, const double* x, double* y, size_t rhs) {
         cudaSuccess)
         return cuda_fail(e, "cudaMemcpy device-to-host");
     if ((e = cudaStreamSynchronize(mm->stream)) != cudaSuccess) return cuda_fail(e, "CUDA kernel execution");
-    if (*mm->h_status) return fail(QH_EINVAL, "nonfinite right-hand side");
+    if (*mm->h_status & kStatusNonfinite) return fail(QH_EINVAL, "nonfinite right-hand side");
+    if (*mm->h_status & kStatusTimeout) return fail(QH_ERUNTIME, "device copy wait timed out");
     std::memcpy(y, mm->pinned, vec);
     return QH_OK;
 }
