@@ -472,12 +472,12 @@ Layout build_layout(const HostMatrix& m) {
                     it.words = int32_t(total);
                     const size_t base = pwords.size();
                     pwords.resize(base + total, 0);
-                    auto* hdr = reinterpret_cast<uint8_t*>(pwords.data() + base);
+                    auto* hdr = reinterpret_cast<uint16_t*>(pwords.data() + base);
                     size_t o = base + kRowHeaderWords;
                     for (uint64_t j = j0; j < j1; ++j) {
                         const uint64_t c = b.comp0 + j;
                         const int w = m.width[c];
-                        hdr[j - j0] = uint8_t(w);
+                        hdr[j - j0] = uint16_t(((o - base) << 5) | uint64_t(w - 1));
                         copy_bits(m.left_words.data() + m.left_off[c], words_for_bits(rows_b, w),
                                   uint64_t(rloc0) * w, uint64_t(rows) * w, pwords.data() + o);
                         o += words_for_bits(uint64_t(rows), w);

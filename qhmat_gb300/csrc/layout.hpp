@@ -109,10 +109,11 @@ struct ColTask {
 // one row tile, or a column slice of one dense block for one row tile (dense:
 // comp = slice index, count = columns, words = first column, off = element
 // offset of (first row, first column) in the column-major values).  Low-rank
-// data block at pwords[off]: 8 header words holding the `count` widths (one
-// byte each), then the pieces (component j's piece = bits [rloc0*w, (rloc0 +
-// rows)*w) of its run, from a fresh word, ceil(rows*w/32) words); `words` is
-// the block's total size, a multiple of 4 words, 16-byte aligned.
+// data block at pwords[off]: kRowHeaderWords header words holding, for each
+// of the `count` components, a 16-bit entry (piece offset in words << 5) |
+// (width - 1); then the pieces (component j's piece = bits [rloc0*w,
+// (rloc0 + rows)*w) of its run, from a fresh word, ceil(rows*w/32) words);
+// `words` is the block's total size, a multiple of 4 words, 16-byte aligned.
 struct RowItem {
     int32_t block;     // >= 0: low-rank block index; < 0: -1 - dense block index
     int32_t rloc0;     // tile row0 - block row0
@@ -133,8 +134,8 @@ struct RowTile {
 constexpr int kStageWordBytes = 4096;
 // Longest run of chunks one column unit walks.
 constexpr int kMaxPartChunks = 16;
-// Header words of a row data block (32 widths, one byte each).
-constexpr int kRowHeaderWords = 8;
+// Header words of a row data block (32 16-bit offset/width entries).
+constexpr int kRowHeaderWords = 16;
 // Column slices a dense diagonal block is cut into (one per row-side warp).
 constexpr int kDenseSlices = 8;
 

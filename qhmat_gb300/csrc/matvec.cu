@@ -125,6 +125,7 @@ struct Arena {
 
 struct Work {
     double* xc;        // [rhs][n]  x in clustered order (FP64)
+    int2* xl;          // [rhs][n]  x in fixed point on its column's exponent, two limbs
     int* xe;           // [rhs]     largest exponent field of x (zeroed before prep_x)
     int* split_cnt;    // [n_split][rhs] finished parts of each split column task (zeroed)
     long long* part;   // [n_split][max_parts][rhs][32][2] partial sums of split tasks
@@ -286,21 +287,29 @@ __global__ void __launch_bounds__(256) prep_x_kernel(Arena A, Work W, const doub
     if (lane == 0 && emax) atomicMax(W.xe + p, emax);
 }
 
+// x in fixed point on its column's exponent (one thread per entry), after
+// prep_x_kernel has found the exponent.
+__global__ void __launch_bounds__(256) x_limbs_kernel(Work W, int n, int rhs) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)n * rhs) return;
+    const int p = int(i / n);
+    const int xe = W.xe[p];
+    const long long X = xe ? to_fixed(W.xc[i], xe) : 0;
+    W.xl[i] = make_int2(int(X & kLimbMask), int(X >> kLimb));
+}
+
 // sum_{e<NE} code_e * X_e for NE codes held in registers w[], decoded as
 // consumed.
 template <int W, int NE>
 __device__ __forceinline__ void codes_mac(const uint32_t* w, const int2* sX, long long& alo, long long& ahi) {
     // four independent accumulator pairs keep the multiply-add chains short
     long long l[4] = {0, 0, 0, 0}, h[4] = {0, 0, 0, 0};
-    const int4* sX2 = reinterpret_cast<const int4*>(sX);
 #pragma unroll
-    for (int e = 0; e < NE; e += 2) {
-        const int4 xx = sX2[e >> 1];
-        const int c0 = code_at<W>(w, e), c1 = code_at<W>(w, e + 1);
-        l[e & 3] += (long long)c0 * xx.x;
-        h[e & 3] += (long long)c0 * xx.y;
-        l[(e + 1) & 3] += (long long)c1 * xx.z;
-        h[(e + 1) & 3] += (long long)c1 * xx.w;
+    for (int e = 0; e < NE; ++e) {
+        const int2 xx = sX[e];
+        const int c = code_at<W>(w, e);
+        l[e & 3] += (long long)c * xx.x;
+        h[e & 3] += (long long)c * xx.y;
     }
     alo += (l[0] + l[1]) + (l[2] + l[3]);
     ahi += (h[0] + h[1]) + (h[2] + h[3]);
@@ -385,12 +394,10 @@ __device__ __forceinline__ int col_step_chunks(int stride, int remaining) {
 __global__ void __launch_bounds__(kWarps * 32, 2) column_kernel(Arena A, Work W, int n_tasks, int n, int rhs,
                                                                 int n_comp, int max_parts, int* status) {
     extern __shared__ __align__(16) uint8_t smem_raw[];
-    __shared__ __align__(16) int2 sXall[kWarps][kColChunk];
     __shared__ __align__(8) uint64_t s_bar[kWarps][kStages];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint8_t* slots = smem_raw + (size_t)warp * kStages * kSlotBytes;
     uint64_t* bar = s_bar[warp];
-    int2* sX = sXall[warp];
     if (lane == 0) {
         for (int i = 0; i < kStages; ++i) mbar_init(bar + i, 1);
         mbar_init_fence();
@@ -419,7 +426,7 @@ __global__ void __launch_bounds__(kWarps * 32, 2) column_kernel(Arena A, Work W,
             const unsigned wbytes = unsigned(nc * di.stride * 4);
             const int k0 = (di.chunk0 + ic) * kColChunk;
             const int cnt = min(di.n - k0, nc * kColChunk);
-            const double* xa = W.xc + (long long)ip * n + di.col0 + k0;
+            const int2* xa = W.xl + (long long)ip * n + di.col0 + k0;
             const int xs = int((reinterpret_cast<uintptr_t>(xa) >> 3) & 1);
             const unsigned xbytes = unsigned(((cnt + xs) * 8 + 15) & ~15);
             if (lane == 0) {
@@ -459,18 +466,13 @@ __global__ void __launch_bounds__(kWarps * 32, 2) column_kernel(Arena A, Work W,
             const int nc = col_step_chunks(dc.stride, dc.nchunks - cc);
             const uint8_t* slot = slots + slot_i * kSlotBytes;
             const uint32_t* sw = reinterpret_cast<const uint32_t*>(slot);
-            const double* xa = W.xc + (long long)cp * n + dc.col0 + (dc.chunk0 + cc) * kColChunk;
+            const int2* xa = W.xl + (long long)cp * n + dc.col0 + (dc.chunk0 + cc) * kColChunk;
             const int xs = int((reinterpret_cast<uintptr_t>(xa) >> 3) & 1);
-            const double* sv = reinterpret_cast<const double*>(slot + nc * dc.stride * 4) + xs;
+            const int2* sxs = reinterpret_cast<const int2*>(slot + nc * dc.stride * 4) + xs;
             for (int c = 0; c < nc; ++c) {
-                // the chunk's x entries on the column's exponent, as limbs
-                {
-                    const int k = (dc.chunk0 + cc + c) * kColChunk + lane;
-                    long long X = 0;
-                    if (k < dc.n && xe) X = to_fixed(sv[c * kColChunk + lane], xe);
-                    sX[lane] = make_int2(int(X & kLimbMask), int(X >> kLimb));
-                }
-                __syncwarp();
+                // x limbs of the chunk's entries (entries past the range meet
+                // zero codes)
+                const int2* sX = sxs + c * kColChunk;
                 if (lane < dc.count) {
                     const uint32_t* cw = sw + c * dc.stride;
                     long long alo = 0, ahi = 0;
@@ -490,7 +492,6 @@ __global__ void __launch_bounds__(kWarps * 32, 2) column_kernel(Arena A, Work W,
                     }
                     acc += widen(ahi, alo);
                 }
-                __syncwarp();
             }
             ++computed;
             cc += nc;
@@ -696,24 +697,17 @@ __global__ void __launch_bounds__(kWarps * 32, 2) row_kernel(Arena A, Work W, do
                         const double* SV = reinterpret_cast<const double*>(slot + off + d.words * 4) + us;
                         off += d.words * 4 + ((d.count + 1) * 8 + 15) / 16 * 16;
                         // widths from the header, u from the slot
-                        int wl = 0;
+                        int hw = 0;
                         double uv = 0.0;
                         if (lane < d.count) {
-                            wl = int((SW[lane >> 2] >> (8 * (lane & 3))) & 0xFFu);
+                            hw = int((SW[lane >> 1] >> (16 * (lane & 1))) & 0xFFFFu);
                             uv = SV[lane];
                         }
                         const int eb = __reduce_max_sync(0xFFFFFFFFu, lane < d.count ? exp_field(uv) : 0);
                         if (eb) {
                             const long long U = lane < d.count ? to_fixed(uv, eb) : 0;
-                            const int sz = (T.rows * wl + 31) >> 5;
-                            int incl = sz;
-#pragma unroll
-                            for (int o = 1; o < 32; o <<= 1) {
-                                const int v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-                                if (lane >= o) incl += v;
-                            }
                             int4* tab = s_tab[warp];
-                            tab[lane] = make_int4(int(U & kLimbMask), int(U >> kLimb), kRowHeaderWords + incl - sz, wl);
+                            tab[lane] = make_int4(int(U & kLimbMask), int(U >> kLimb), hw >> 5, (hw & 31) + 1);
                             __syncwarp();
                             long long alo0 = 0, ahi0 = 0, alo1 = 0, ahi1 = 0;
                             long long blo0 = 0, bhi0 = 0, blo1 = 0, bhi1 = 0;
@@ -870,15 +864,15 @@ __global__ void decode_row_kernel(Arena A, int n_tiles, const long long* __restr
             const RowItem I = A.items[it];
             if (I.block < 0) continue;
             const uint32_t* blk = A.pwords + I.off;
-            const uint32_t* piece = blk + kRowHeaderWords;
             for (int j = 0; j < I.count; ++j) {
-                const int w = int((blk[j >> 2] >> (8 * (j & 3))) & 0xFFu);
+                const int hw = int((blk[j >> 1] >> (16 * (j & 1))) & 0xFFFFu);
+                const int w = (hw & 31) + 1;
+                const uint32_t* piece = blk + (hw >> 5);
                 int c0 = 0, c1 = 0;
                 if (2 * lane < T.rows) row_pair_codes_rt(piece, lane, w, c0, c1);
                 const long long o = comp_off[I.comp + j] + I.rloc0;
                 if (2 * lane < T.rows) out[o + 2 * lane] = c0;
                 if (2 * lane + 1 < T.rows) out[o + 2 * lane + 1] = c1;
-                piece += (T.rows * w + 31) >> 5;
             }
         }
     }
@@ -1023,7 +1017,7 @@ int guarded(F&& f) {
 }
 
 struct WsPlan {
-    size_t xc, xe, cnt, part, u, total, zero_bytes;
+    size_t xc, xl, xe, cnt, part, u, total, zero_bytes;
 };
 
 WsPlan ws_plan(const Layout& L, size_t rhs) {
@@ -1040,6 +1034,7 @@ WsPlan ws_plan(const Layout& L, size_t rhs) {
     w.zero_bytes = off;
     // xc and u are read by 16-byte-rounded bulk copies: keep 32 spare bytes
     w.xc = take(8 * L.order * rhs + 32);
+    w.xl = take(8 * L.order * rhs + 32);
     w.part = take(16 * 32 * size_t(L.n_split) * size_t(L.max_parts) * rhs);
     w.u = take(8 * size_t(L.n_comp) * rhs + 32);
     w.total = off;
@@ -1056,6 +1051,7 @@ int launch(const qh_matrix* m, const double* x, double* y, size_t rhs, void* ws,
     const WsPlan P = ws_plan(L, rhs);
     Work W;
     W.xc = reinterpret_cast<double*>(w + P.xc);
+    W.xl = reinterpret_cast<int2*>(w + P.xl);
     W.xe = reinterpret_cast<int*>(w + P.xe);
     W.split_cnt = reinterpret_cast<int*>(w + P.cnt);
     W.part = reinterpret_cast<long long*>(w + P.part);
@@ -1068,6 +1064,7 @@ int launch(const qh_matrix* m, const double* x, double* y, size_t rhs, void* ws,
     cudaError_t e = cudaMemsetAsync(w, 0, P.zero_bytes, s);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
     prep_x_kernel<<<unsigned((prep_warps + 7) / 8), 256, 0, s>>>(m->A, W, x, n, int(rhs), L.n_chunks, status);
+    x_limbs_kernel<<<unsigned(((long long)n * (long long)rhs + 255) / 256), 256, 0, s>>>(W, n, int(rhs));
     mark(1);
     if (L.n_tasks > 0) {
         const int grid = std::max(1, std::min((L.n_tasks + kWarps - 1) / kWarps, m->sms * 2));
