@@ -271,18 +271,41 @@ T* at(std::vector<uint8_t>& arena, size_t off) {
 // Copy the bit string [bit0, bit0 + nbits) of a run of `run_words` words to
 // out[0 .. ceil(nbits/32)), starting at a fresh word; bits past the string
 // (or past the run) are zero.
-void copy_bits(const uint32_t* run, uint64_t run_words, uint64_t bit0, uint64_t nbits, uint32_t* out) {
-    const uint64_t nw = (nbits + 31) / 32;
-    for (uint64_t i = 0; i < nw; ++i) {
-        const uint64_t b = bit0 + 32 * i;
-        const uint64_t wi = b >> 5;
-        const unsigned sh = unsigned(b & 31);
-        const uint64_t lo = wi < run_words ? run[wi] : 0;
-        const uint64_t hi = wi + 1 < run_words ? run[wi + 1] : 0;
-        uint32_t v = uint32_t(((hi << 32) | lo) >> sh);
-        const uint64_t rem = nbits - 32 * i;
-        if (rem < 32) v &= (1u << rem) - 1u;
-        out[i] = v;
+// Code i of a component's run: bits [i*w, i*w + w), LSB-first, sign-extended
+// -- the field HMatrix::decode reads (src/qhmat/core.cpp:269-282).
+int32_t code_of(const uint32_t* run, uint64_t i, int w) {
+    const uint64_t pos = i * uint64_t(w), wi = pos >> 5, off = pos & 31;
+    uint64_t v = run[wi];
+    if (off + uint64_t(w) > 32) v |= uint64_t(run[wi + 1]) << 32;
+    const uint64_t f = (v >> off) & ((uint64_t(1) << w) - 1);
+    return int32_t(int64_t(f << (64 - w)) >> (64 - w));
+}
+
+// Offset code u = c + 2^(w-1) in [0, 2^w).
+inline uint32_t offset_code(int32_t c, int w) { return uint32_t(int64_t(c) + (int64_t(1) << (w - 1))); }
+
+// Position of k-block kb entry e (0..15) inside a fragment row: thread t and
+// slot s (0..3: entries 2t, 2t+1, 2t+8, 2t+9).
+inline void frag_pos(int e, int& t, int& slot) {
+    t = (e & 7) >> 1;
+    slot = (e & 1) | ((e >> 3) << 1);
+}
+
+// Store digit d of (k-block kb, entry e) into a group row at `row` (32 bytes
+// for a byte group, 16 for a nibble group).
+inline void put_digit(uint8_t* row, bool nib, int kb, int e, uint32_t d) {
+    int t, slot;
+    frag_pos(e, t, slot);
+    if (!nib) {
+        row[8 * t + 4 * kb + slot] = uint8_t(d);
+    } else {
+        // register k = 2kb + (slot >> 1) of the pair: low half nibble k, high
+        // half nibble k + 4
+        const int nibble = 2 * kb + (slot >> 1) + 4 * (slot & 1);
+        uint32_t w;
+        std::memcpy(&w, row + 4 * t, 4);
+        w |= (d & 15u) << (4 * nibble);
+        std::memcpy(row + 4 * t, &w, 4);
     }
 }
 
@@ -334,6 +357,10 @@ Layout build_layout(const HostMatrix& m) {
     L.n_chunks = int32_t((m.order + kChunk - 1) / kChunk);
 
     // ---- column side: tasks of <= 32 components sharing (col0, n, width).
+    // beta[c]: |u_c| < 2^(xe - 1022 + beta[c]) for x whose exponent fields are
+    // <= xe (|u| <= |s^P s^Q| * ||c^Q||_1 * max|x|, one binade of slack for
+    // rounding); kNoExp when u is identically zero.
+    std::vector<int32_t> beta(m.width.size(), kNoExp);
     struct Key {
         int32_t col0, n, w;
         bool operator<(const Key& o) const {
@@ -349,8 +376,9 @@ Layout build_layout(const HostMatrix& m) {
     std::stable_sort(comps.begin(), comps.end(),
                      [](const auto& a, const auto& b) { return a.first < b.first; });
     std::vector<ColTask> tasks;
-    std::vector<int32_t> task_comp;
-    std::vector<uint32_t> qwords;
+    std::vector<TaskRec> task_rec;
+    std::vector<int32_t> comp_part(m.width.size(), -1);  // row of a split task's partial sums, or -1
+    std::vector<uint8_t> qcodes;
     int32_t n_split = 0;
     for (size_t i = 0; i < comps.size();) {
         size_t j = i;
@@ -358,32 +386,61 @@ Layout build_layout(const HostMatrix& m) {
         for (size_t t0 = i; t0 < j; t0 += 32) {
             const int32_t count = int32_t(std::min<size_t>(32, j - t0));
             const Key key = comps[t0].first;
+            const int P = code_planes(key.w);
+            const bool nibtop = top_is_nibble(key.w);
+            const int32_t row_bytes = (P - 1) * 32 + (nibtop ? 16 : 32);  // one row, all planes
+            const int32_t stride = count * row_bytes;
             const int32_t nchunks = (key.n + kColChunk - 1) / kColChunk;
-            const int32_t stride = (count * key.w + 3) / 4 * 4;
-            const int32_t comp_idx = int32_t(task_comp.size());
-            for (int32_t l = 0; l < count; ++l) task_comp.push_back(comps[t0 + l].second);
-            const size_t base = qwords.size();  // multiple of 4 words
-            qwords.resize(base + size_t(nchunks) * stride, 0);
+            const int32_t comp_idx = int32_t(task_rec.size());
             for (int32_t l = 0; l < count; ++l) {
                 const int32_t c = comps[t0 + l].second;
-                const uint32_t* run = m.right_words.data() + m.right_off[c];
-                const uint64_t run_words = words_for_bits(uint64_t(key.n), key.w);
-                for (int32_t ch = 0; ch < nchunks; ++ch)
-                    for (int32_t v = 0; v < key.w; ++v) {
-                        const uint64_t wi = uint64_t(ch) * key.w + v;
-                        qwords[base + size_t(ch) * stride + size_t(v) * count + l] = wi < run_words ? run[wi] : 0u;
+                // One rounding: s_P * s_Q.  In exact arithmetic the block contribution
+                // sum_j (s_P c_P)(sum_k s_Q c_Q x) equals sum_j c_P (s_P s_Q) sum_k c_Q x.
+                task_rec.push_back({c, key.w, m.left_scale[size_t(c)] * m.right_scale[size_t(c)]});
+            }
+            const size_t base = qcodes.size();  // multiple of 16 bytes
+            qcodes.resize(base + size_t(nchunks) * size_t(stride), 0);
+            for (int32_t l = 0; l < count; ++l) {
+                const int32_t c = comps[t0 + l].second;
+                const uint32_t* run = m.right_words.data() + m.right_off[size_t(c)];
+                const int q = l / 16, r = l % 16;
+                const int rows_q = std::min<int32_t>(16, count - 16 * q);
+                double l1 = 0.0;
+                for (int32_t ch = 0; ch < nchunks; ++ch) {
+                    // group (q, mm) of chunk ch starts after the earlier M-tile's groups
+                    size_t goff = base + size_t(ch) * size_t(stride) + size_t(q) * 16 * size_t(row_bytes);
+                    for (int mm = 0; mm < P; ++mm) {
+                        const bool nb = nibtop && mm == P - 1;
+                        const size_t rb = nb ? 16 : 32;
+                        uint8_t* row = qcodes.data() + goff + size_t(r) * rb;
+                        for (int e = 0; e < kColChunk; ++e) {
+                            // entries past the range hold code 0 (every digit
+                            // of it reads as zero on the device)
+                            const int64_t idx = int64_t(ch) * kColChunk + e;
+                            const int32_t code = idx < key.n ? code_of(run, uint64_t(idx), key.w) : 0;
+                            if (mm == 0) l1 += std::fabs(double(code));
+                            const uint32_t u = offset_code(code, key.w);
+                            put_digit(row, nb, e >> 4, e & 15, (u >> (8 * mm)) & (nb ? 15u : 255u));
+                        }
+                        goff += size_t(rows_q) * rb;
                     }
+                }
+                const double bound = l1 * std::fabs(m.left_scale[size_t(c)] * m.right_scale[size_t(c)]);
+                if (bound > 0.0 && std::isfinite(bound)) beta[size_t(c)] = int32_t(std::ilogb(bound)) + 2;
             }
             const int32_t nparts = (nchunks + kMaxPartChunks - 1) / kMaxPartChunks;
             const int32_t split_id = nparts > 1 ? n_split++ : -1;
+            if (split_id >= 0)
+                for (int32_t l = 0; l < count; ++l) comp_part[size_t(comps[t0 + l].second)] = split_id * 32 + l;
             L.max_parts = std::max(L.max_parts, nparts);
+            const int32_t cps = std::max<int32_t>(1, kColSlotBytes / (stride + kColChunk * 16));
             for (int32_t pt = 0; pt < nparts; ++pt) {
                 ColTask T{};
                 T.col0 = key.col0;
                 T.n = key.n;
-                T.width = key.w;
                 T.count = count;
-                T.word0 = int64_t(base);
+                T.width = key.w;
+                T.off = int64_t(base);
                 T.stride = stride;
                 T.comp_idx = comp_idx;
                 T.chunk0 = pt * kMaxPartChunks;
@@ -391,6 +448,7 @@ Layout build_layout(const HostMatrix& m) {
                 T.part = pt;
                 T.nparts = nparts;
                 T.split_id = split_id;
+                T.cps = cps;
                 tasks.push_back(T);
             }
         }
@@ -398,11 +456,11 @@ Layout build_layout(const HostMatrix& m) {
     }
     // heaviest units first
     std::stable_sort(tasks.begin(), tasks.end(), [](const ColTask& a, const ColTask& b) {
-        return int64_t(a.nchunks) * a.width * a.count > int64_t(b.nchunks) * b.width * b.count;
+        return int64_t(a.nchunks) * (a.stride + 512) > int64_t(b.nchunks) * (b.stride + 512);
     });
     L.n_tasks = int32_t(tasks.size());
     L.n_split = n_split;
-    L.stored_q_words = qwords.size();
+    L.stored_q_bytes = qcodes.size();
 
     // ---- row side: elementary slabs (finalize's row boundaries) cut into tiles.
     std::vector<uint64_t> bounds{0, m.order};
@@ -419,94 +477,157 @@ Layout build_layout(const HostMatrix& m) {
         size_t s = size_t(std::lower_bound(bounds.begin(), bounds.end(), b.row0) - bounds.begin());
         for (; s < n_slabs && bounds[s] < b.row1; ++s) slab_blocks[s].push_back(int32_t(k));
     }
-    std::vector<RowItem> items;
     std::vector<RowTile> tiles;
-    std::vector<int64_t> tile_work;
-    std::vector<uint32_t> pwords;
-    const uint64_t max_block_words = kStageWordBytes / 4;
+    std::vector<std::pair<int64_t, RowUnit>> units;  // (cost, unit)
+    std::vector<uint8_t> pcodes;
+    std::vector<uint8_t> kp_info;
+    int64_t n_slots = 0;
+    int32_t n_dense_parts = 0;
+    std::vector<int32_t> slot_comp;  // component of each B row slot (-1: padding)
+    std::vector<int32_t> kpg_tile;   // tile of each B row group
+    struct RowComp {
+        int w;
+        int32_t comp;
+        int32_t block;  // index into m.blocks
+    };
     for (size_t s = 0; s < n_slabs; ++s) {
         for (uint64_t r = bounds[s]; r < bounds[s + 1]; r += kTileRows) {
             const int32_t rows = int32_t(std::min<uint64_t>(kTileRows, bounds[s + 1] - r));
-            RowTile T{int32_t(r), rows, int32_t(items.size()), 0};
-            int64_t work = 0;
-            std::vector<std::pair<int64_t, RowItem>> units;  // (cost, unit)
+            const int32_t ti = int32_t(tiles.size());
+            RowTile T{};
+            T.row0 = int32_t(r);
+            T.rows = rows;
+            T.dense0 = n_dense_parts;
+            std::vector<RowComp> kc;
             for (int32_t k : slab_blocks[s]) {
                 const auto& b = m.blocks[size_t(k)];
                 const int32_t rloc0 = int32_t(r - b.row0);
                 if (b.dense) {
-                    // column slices, one per warp, summed in slice order
+                    // column slices, one unit each, summed in slice order
                     const DenseDesc& d = dd[size_t(-1 - block_item[size_t(k)])];
                     const int32_t ns = std::min<int32_t>(kDenseSlices, d.n);
                     for (int32_t sl = 0; sl < ns; ++sl) {
                         const int32_t c0 = int32_t(int64_t(d.n) * sl / ns), c1 = int32_t(int64_t(d.n) * (sl + 1) / ns);
-                        RowItem it{};
-                        it.block = block_item[size_t(k)];
-                        it.rloc0 = rloc0;
-                        it.comp = sl;          // slice index
-                        it.count = c1 - c0;    // columns in the slice
-                        it.off = d.off + int64_t(c0) * d.m + rloc0;
-                        it.words = c0;         // first column of the slice
-                        const int64_t cost = int64_t(rows) * (c1 - c0) * 16;
-                        units.push_back({cost, it});
-                        work += cost;
+                        RowUnit U{};
+                        U.tile = ti;
+                        U.kind = 1;
+                        U.h = n_dense_parts + T.nslices;
+                        U.cols = c1 - c0;
+                        U.ld = d.m;
+                        U.xcol = d.col0 + c0;
+                        U.rows = rows;
+                        U.doff = d.off + int64_t(c0) * d.m + rloc0;
+                        units.push_back({int64_t(rows) * (c1 - c0) * 8, U});
+                        ++T.nslices;
                     }
                     continue;
                 }
-                const uint64_t rows_b = b.row1 - b.row0;
-                for (uint64_t j0 = 0; j0 < b.rank;) {
-                    // greedy group: <= 32 components whose pieces fit one stage
-                    uint64_t j1 = j0, words = kRowHeaderWords;
-                    while (j1 < b.rank && j1 - j0 < 32) {
-                        const uint64_t pw = words_for_bits(uint64_t(rows), m.width[b.comp0 + j1]);
-                        if (words + pw > max_block_words) break;
-                        words += pw;
-                        ++j1;
-                    }
-                    RowItem it{};
-                    it.block = block_item[size_t(k)];
-                    it.rloc0 = rloc0;
-                    it.comp = int32_t(b.comp0 + j0);
-                    it.count = int32_t(j1 - j0);
-                    it.off = int64_t(pwords.size());
-                    const uint64_t total = (words + 3) / 4 * 4;
-                    it.words = int32_t(total);
-                    const size_t base = pwords.size();
-                    pwords.resize(base + total, 0);
-                    auto* hdr = reinterpret_cast<uint16_t*>(pwords.data() + base);
-                    size_t o = base + kRowHeaderWords;
-                    for (uint64_t j = j0; j < j1; ++j) {
-                        const uint64_t c = b.comp0 + j;
-                        const int w = m.width[c];
-                        hdr[j - j0] = uint16_t(((o - base) << 5) | uint64_t(w - 1));
-                        copy_bits(m.left_words.data() + m.left_off[c], words_for_bits(rows_b, w),
-                                  uint64_t(rloc0) * w, uint64_t(rows) * w, pwords.data() + o);
-                        o += words_for_bits(uint64_t(rows), w);
-                    }
-                    const int64_t cost = int64_t(rows) * int64_t(j1 - j0) + 64;
-                    units.push_back({cost, it});
-                    work += cost;
-                    j0 = j1;
-                }
+                for (uint64_t j = 0; j < b.rank; ++j)
+                    kc.push_back({int(m.width[b.comp0 + j]), int32_t(b.comp0 + j), k});
             }
-            // heaviest first: the tile's warps take units round-robin
-            std::stable_sort(units.begin(), units.end(),
-                             [](const auto& a, const auto& b) { return a.first > b.first; });
-            for (const auto& u : units) items.push_back(u.second);
-            T.item1 = int32_t(items.size());
+            std::stable_sort(kc.begin(), kc.end(), [](const RowComp& a, const RowComp& b) { return a.w > b.w; });
+            const int32_t K = int32_t(kc.size());
+            const int32_t Kp = (K + 31) / 32;
+            T.qrows = (rows + 15) / 16;
+            T.hsplit = T.qrows == 1 ? 8 : (T.qrows == 2 ? 4 : 2);
+            T.nh = std::min(T.hsplit, Kp);
+            T.c_exp = kNoExp;
+            for (const auto& c : kc) T.c_exp = std::max(T.c_exp, beta[size_t(c.comp)]);
+            const int64_t kp_off = int64_t(kp_info.size());
+            // per k-pair: planes and nibble planes
+            std::vector<int> kplanes(static_cast<size_t>(Kp), 0), knib(static_cast<size_t>(Kp), 0);
+            for (int32_t kp = 0; kp < Kp; ++kp) {
+                int planes = 0, nibs = 0;
+                for (int mm = 0; mm < 4; ++mm) {
+                    bool any = false, all_nib = true;
+                    for (int32_t k = 32 * kp; k < std::min(K, 32 * kp + 32); ++k) {
+                        const int w = kc[size_t(k)].w;
+                        if (code_planes(w) > mm) {
+                            any = true;
+                            if (!(code_planes(w) == mm + 1 && top_is_nibble(w))) all_nib = false;
+                        }
+                    }
+                    if (any) {
+                        planes = mm + 1;
+                        if (all_nib) nibs |= 1 << mm;
+                    }
+                }
+                kplanes[size_t(kp)] = planes;
+                knib[size_t(kp)] = nibs;
+                kp_info.push_back(uint8_t(planes | (nibs << 3)));
+            }
+            // B row slots: k split h's k-pairs contiguously
+            std::vector<int64_t> hslot(size_t(T.hsplit), 0);
+            T.kpg0 = int32_t(n_slots / 32);
+            for (int32_t h = 0; h < T.nh; ++h) {
+                hslot[size_t(h)] = n_slots;
+                for (int32_t kp = h; kp < Kp; kp += T.hsplit) {
+                    for (int e = 0; e < 32; ++e) {
+                        const int32_t k = 32 * kp + e;
+                        slot_comp.push_back(k < K ? kc[size_t(k)].comp : -1);
+                    }
+                    kpg_tile.push_back(ti);
+                }
+                n_slots += 32 * int64_t((Kp - h + T.hsplit - 1) / T.hsplit);
+            }
+            T.nkpg = int32_t(n_slots / 32) - T.kpg0;
+            // streams (q, h): groups of 16 rows
+            for (int32_t q = 0; q < T.qrows; ++q)
+                for (int32_t h = 0; h < T.nh; ++h) {
+                    RowUnit U{};
+                    U.tile = ti;
+                    U.kind = 0;
+                    U.q = q;
+                    U.h = h;
+                    U.H = T.hsplit;
+                    U.nkps = (Kp - h + T.hsplit - 1) / T.hsplit;
+                    U.K = K;
+                    U.slot0 = int32_t(hslot[size_t(h)]);
+                    U.code_off = int64_t(pcodes.size());
+                    U.kp_off = kp_off;
+                    int64_t bytes = 0;
+                    for (int32_t kp = h; kp < Kp; kp += T.hsplit)
+                        for (int mm = 0; mm < kplanes[size_t(kp)]; ++mm) {
+                            const bool nb = (knib[size_t(kp)] >> mm) & 1;
+                            const size_t rb = nb ? 16 : 32;
+                            const size_t g0 = pcodes.size();
+                            pcodes.resize(g0 + 16 * rb, 0);
+                            for (int rr = 0; rr < 16; ++rr) {
+                                const int32_t tr = 16 * q + rr;  // tile row
+                                if (tr >= rows) break;
+                                uint8_t* row = pcodes.data() + g0 + size_t(rr) * rb;
+                                for (int e = 0; e < 32; ++e) {
+                                    const int32_t k = 32 * kp + e;
+                                    if (k >= K) break;
+                                    const RowComp& c = kc[size_t(k)];
+                                    const auto& b = m.blocks[size_t(c.block)];
+                                    const uint32_t* run = m.left_words.data() + m.left_off[size_t(c.comp)];
+                                    const uint64_t br = r + uint64_t(tr) - b.row0;
+                                    const uint32_t u = offset_code(code_of(run, br, c.w), c.w);
+                                    put_digit(row, nb, e >> 4, e & 15, (u >> (8 * mm)) & (nb ? 15u : 255u));
+                                }
+                            }
+                            bytes += int64_t(16 * rb);
+                        }
+                    units.push_back({bytes + int64_t(U.nkps) * 512, U});
+                }
+            n_dense_parts += T.nslices;
+            if (T.qrows * T.nh + T.nslices == 0) throw runtime_error("row tile without blocks");
             tiles.push_back(T);
-            tile_work.push_back(work);
         }
     }
-    std::vector<int32_t> torder(tiles.size());
-    std::iota(torder.begin(), torder.end(), 0);
-    std::stable_sort(torder.begin(), torder.end(),
-                     [&](int32_t a, int32_t b) { return tile_work[a] > tile_work[b]; });
-    std::vector<RowTile> tiles_sorted(tiles.size());
-    for (size_t i = 0; i < tiles.size(); ++i) tiles_sorted[i] = tiles[torder[i]];
+    if (n_slots >= (int64_t(1) << 31)) throw overflow_error("too many row-side slots for the device layout");
+    // heaviest units first: the warps take them round-robin
+    std::stable_sort(units.begin(), units.end(), [](const auto& a, const auto& b) { return a.first > b.first; });
+    std::vector<RowUnit> unit_list;
+    for (const auto& u : units) unit_list.push_back(u.second);
     L.n_tiles = int32_t(tiles.size());
-    L.n_items = int32_t(items.size());
-    L.stored_p_words = pwords.size();
-    if (qwords.size() >= (1ull << 40) || pwords.size() >= (1ull << 40))
+    L.n_kpg = int32_t(kpg_tile.size());
+    L.n_units = int32_t(unit_list.size());
+    L.n_slots = int32_t(n_slots);
+    L.n_dense_parts = n_dense_parts;
+    L.stored_p_bytes = pcodes.size();
+    if (qcodes.size() >= (1ull << 42) || pcodes.size() >= (1ull << 42))
         throw overflow_error("packed factors too large for the device layout");
 
     // ---- arena sections, each 256-byte aligned.
@@ -524,12 +645,16 @@ Layout build_layout(const HostMatrix& m) {
     S.comp_w = place(C);
     S.comp_s = place(8 * C);
     S.tasks = place(sizeof(ColTask) * tasks.size());
-    S.task_comp = place(4 * task_comp.size());
-    S.qwords = place(4 * qwords.size() + 16);
-    S.pwords = place(4 * pwords.size() + 16);
+    S.task_rec = place(sizeof(TaskRec) * task_rec.size());
+    S.qcodes = place(qcodes.size() + 16);
+    S.pcodes = place(pcodes.size() + 16);
     S.dense = place(8 * dense_cm.size());
     S.tiles = place(sizeof(RowTile) * tiles.size());
-    S.items = place(sizeof(RowItem) * items.size());
+    S.units = place(sizeof(RowUnit) * unit_list.size());
+    S.kp_info = place(kp_info.size() + 16);
+    S.slot_comp = place(4 * slot_comp.size());
+    S.kpg_tile = place(4 * kpg_tile.size());
+    S.comp_part = place(4 * comp_part.size());
     S.total = off;
 
     L.arena.assign(S.total, 0);
@@ -544,13 +669,16 @@ Layout build_layout(const HostMatrix& m) {
         at<double>(A, S.comp_s)[c] = m.left_scale[c] * m.right_scale[c];
     }
     if (!tasks.empty()) std::memcpy(at<ColTask>(A, S.tasks), tasks.data(), sizeof(ColTask) * tasks.size());
-    if (!task_comp.empty()) std::memcpy(A.data() + S.task_comp, task_comp.data(), 4 * task_comp.size());
-    if (!qwords.empty()) std::memcpy(A.data() + S.qwords, qwords.data(), 4 * qwords.size());
-    if (!pwords.empty()) std::memcpy(A.data() + S.pwords, pwords.data(), 4 * pwords.size());
+    if (!task_rec.empty()) std::memcpy(A.data() + S.task_rec, task_rec.data(), sizeof(TaskRec) * task_rec.size());
+    if (!qcodes.empty()) std::memcpy(A.data() + S.qcodes, qcodes.data(), qcodes.size());
+    if (!pcodes.empty()) std::memcpy(A.data() + S.pcodes, pcodes.data(), pcodes.size());
+    if (!kp_info.empty()) std::memcpy(A.data() + S.kp_info, kp_info.data(), kp_info.size());
+    if (!unit_list.empty()) std::memcpy(A.data() + S.units, unit_list.data(), sizeof(RowUnit) * unit_list.size());
+    if (!slot_comp.empty()) std::memcpy(A.data() + S.slot_comp, slot_comp.data(), 4 * slot_comp.size());
+    if (!kpg_tile.empty()) std::memcpy(A.data() + S.kpg_tile, kpg_tile.data(), 4 * kpg_tile.size());
+    if (!comp_part.empty()) std::memcpy(A.data() + S.comp_part, comp_part.data(), 4 * comp_part.size());
     if (!dense_cm.empty()) std::memcpy(A.data() + S.dense, dense_cm.data(), 8 * dense_cm.size());
-    if (!tiles_sorted.empty())
-        std::memcpy(A.data() + S.tiles, tiles_sorted.data(), sizeof(RowTile) * tiles_sorted.size());
-    if (!items.empty()) std::memcpy(A.data() + S.items, items.data(), sizeof(RowItem) * items.size());
+    if (!tiles.empty()) std::memcpy(A.data() + S.tiles, tiles.data(), sizeof(RowTile) * tiles.size());
     return L;
 }
 

@@ -5,22 +5,38 @@
 // workspace.  Nothing here depends on CUDA, so the builder is unit-testable
 // on the CPU.
 //
-// Code words keep the reference's bit packing (component j of width w_j,
-// LSB-first, code i at bit i*w_j of the component's run) but the 32-bit words
-// are permuted so that each kernel reads them coalesced:
+// Codes are stored as digit planes laid out for the tensor cores.  A code c of
+// width w (two's complement) is offset to u = c + 2^(w-1) in [0, 2^w) and cut
+// into P = ceil(w/8) base-256 digits d_m = (u >> 8m) & 255; the top digit
+// holds t = w - 8(P-1) bits and is stored as a nibble when t <= 4.  Then
+//     sum_i c_i v_i = sum_m 2^(8m) sum_i d_m,i v_i  -  2^(w-1) sum_i v_i,
+// and every inner sum is an exact small-integer product sum (digits <= 255
+// times 8-bit limbs of the fixed-point operand), which the f16 tensor-core
+// MMA computes exactly in FP32 (no partial sum reaches 2^24).  Digits are
+// grouped into the 16x16 A-operand fragments of mma.m16n8k16: within a
+// 16-entry k-block, thread t of a fragment row needs entries 2t, 2t+1, 2t+8,
+// 2t+9, and those four digits are stored together:
+//   byte group row (32 bytes per 2 k-blocks): bytes 8t..8t+3 = k-block 0
+//     entries (2t, 2t+1, 2t+8, 2t+9), bytes 8t+4..8t+7 = k-block 1;
+//   nibble group row (16 bytes per 2 k-blocks): word t, nibble k (k = 0..3:
+//     k-block k>>1, entry 2t + 8(k&1)) and nibble k+4 (the following entry).
 //
-//  * right factor Q (column side): components are grouped into tasks of at
-//    most 32 components that share a column range and a width; lane l of a
-//    warp owns component l of its task.  For chunk c (entries 32c..32c+31)
-//    the chunk's w words of lane l's run sit at
-//        qwords[task.word0 + c*w*count + v*count + l],  v = 0..w-1,
-//    so a warp loading word v of its chunk reads `count` consecutive words.
-//  * left factor P (row side): rows are cut into tiles of at most 64 rows
-//    inside one elementary row slab.  For each (tile, block covering it) the
-//    pieces of the block's components for the tile's rows are stored back to
-//    back: component j's piece is the bit string [r0*w_j, (r0+rows)*w_j) of
-//    its run (r0 = tile row - block row0), starting at a fresh word and
-//    occupying ceil(rows*w_j/32) words.
+//  * right factor Q (column side): components sharing a column range and a
+//    width form tasks of <= 32 (two 16-row M-tiles).  Per 32-entry chunk a
+//    task stores, for each M-tile q and plane m, the group of its rows_q rows;
+//    entries past the range hold code 0.  The device reads the top digit as
+//    signed (d = stored - 2^(t-1)), so the column side needs no correction.
+//  * left factor P (row side): rows are cut into tiles of <= 64 rows inside
+//    one elementary row slab.  The components of all blocks covering a tile
+//    are sorted by width and form the tile's k axis (k-pairs of 32).  The
+//    tile's M-tile q (16 rows) and k split h own one contiguous stream (a row
+//    unit): for every k-pair kp = h, h + H, ... and every plane m of the
+//    k-pair, one group of 16 rows (zero past the tile or past the k axis).
+//    Each k slot has a B row, written for every apply: the eight f16 limbs of
+//    U = u in fixed point on the tile's exponent; a unit's B rows are
+//    contiguous (slot = tile base + h's base + 32 i + lane for its i-th
+//    k-pair), and every 32 slots (a B row group) also get the sum of
+//    2^(w-1) U that corrects the offset codes.
 //  * dense diagonal blocks are stored column-major (value (i, k) at
 //    off + k*m + i) so that lanes owning consecutive rows read consecutive
 //    doubles.
@@ -91,71 +107,93 @@ struct LowRankDesc {
 };
 // Column-side unit of work: chunks [chunk0, chunk0 + nchunks) of a task of
 // `count` (<= 32) components of width `width` whose blocks share the column
-// range [col0, col0 + n).  Chunk c of the task starts at word
-// word0 + c * stride (16-byte aligned; stride = `count * width` rounded up to
-// a multiple of 4 words) and holds word v of lane l at + v * count + l.
-// A task longer than kMaxPartChunks chunks is split into `nparts` parts whose
-// partial sums are combined by the part that finishes last.
+// range [col0, col0 + n).  Chunk c of the task starts at byte off + c * stride
+// and holds, for M-tile q (rows_q = min(16, count - 16q)) and plane m, rows_q
+// rows of 32 bytes (16 for a nibble top plane).  A pipeline step carries
+// `cps` chunks.  A task longer than kMaxPartChunks chunks is split into
+// `nparts` parts whose partial sums are combined by the part that finishes
+// last.
 struct ColTask {
-    int32_t col0, n, width, count;
-    int64_t word0;
-    int32_t stride, comp_idx;   // comp_idx: first of `count` entries in task_comp
+    int32_t col0, n, count, width;
+    int64_t off;
+    int32_t stride, comp_idx;   // comp_idx: first of `count` entries in task_rec
     int32_t chunk0, nchunks;
     int32_t part, nparts;
     int32_t split_id;           // index of the split task (counter / partials), -1 if nparts == 1
-    int32_t pad;
+    int32_t cps;
+    int32_t pad[2];
 };
-// Row-side unit of work: components [j0, j0 + count) of one low-rank block for
-// one row tile, or a column slice of one dense block for one row tile (dense:
-// comp = slice index, count = columns, words = first column, off = element
-// offset of (first row, first column) in the column-major values).  Low-rank
-// data block at pwords[off]: kRowHeaderWords header words holding, for each
-// of the `count` components, a 16-bit entry (piece offset in words << 5) |
-// (width - 1); then the pieces (component j's piece = bits [rloc0*w,
-// (rloc0 + rows)*w) of its run, from a fresh word, ceil(rows*w/32) words);
-// `words` is the block's total size, a multiple of 4 words, 16-byte aligned.
-struct RowItem {
-    int32_t block;     // >= 0: low-rank block index; < 0: -1 - dense block index
-    int32_t rloc0;     // tile row0 - block row0
-    int32_t comp, count;  // first component id (block comp0 + j0), components in the unit
-    int64_t off;       // low-rank: word offset of the data block; dense: element offset
-    int32_t words, pad;
+static_assert(sizeof(ColTask) == 64, "ColTask layout");
+// Finalize operands of one component of a column task (one 16-byte load).
+struct TaskRec {
+    int32_t comp, width;
+    double scale;  // s^P s^Q
 };
 struct DenseDesc {
     int32_t row0, m, col0, n;
     int64_t off;  // element offset of the column-major values in the dense arena
 };
+// One row tile: clustered rows [row0, row0 + rows) inside one slab; qrows
+// M-tiles, k axis split hsplit ways (nh of the splits have k-pairs); dense
+// slices with partial sums dense0 .. dense0 + nslices - 1; B row groups (32
+// slots each) kpg0 .. kpg0 + nkpg - 1; u is put in fixed point on the
+// exponent field xe + c_exp (xe: the largest exponent field of x).
 struct RowTile {
-    int32_t row0, rows;     // clustered rows [row0, row0+rows), inside one slab
-    int32_t item0, item1;   // range in the items array (the tile's units)
+    int32_t row0, rows, qrows, hsplit;
+    int32_t nh, nslices, dense0, c_exp;
+    int32_t kpg0, nkpg, pad[2];
 };
+static_assert(sizeof(RowTile) == 48, "RowTile layout");
+// One warp's unit of row-side work.  kind 0: rows 16q .. 16q + 15 of a tile
+// over the k-pairs kp = h, h + H, ... (nkps of them; B rows from slot0;
+// digit groups from code_off; the tile's k axis has K slots).  kind 1: a
+// column slice of a dense diagonal block: `cols` columns of stride `ld`
+// starting at element doff (first row = the tile's), x entries from xcol,
+// `rows` rows, dense partial index h.
+struct RowUnit {
+    int32_t tile, kind, q, h;
+    int32_t H, nkps, K, slot0;
+    int64_t code_off, kp_off;
+    int32_t cols, ld, xcol, rows;
+    int64_t doff;
+    int32_t pad[2];
+};
+static_assert(sizeof(RowUnit) == 80, "RowUnit layout");
 
-// Shared-memory stage of one warp's prefetch pipeline (bytes of code words).
-constexpr int kStageWordBytes = 4096;
+// Bytes of one column-side shared-memory stage (code groups and x rows of
+// the step's chunks); one row-side stage (code groups and B rows).
+constexpr int kColSlotBytes = 4608;
+constexpr int kRowSlotBytes = 4096;
 // Longest run of chunks one column unit walks.
 constexpr int kMaxPartChunks = 16;
-// Header words of a row data block (32 16-bit offset/width entries).
-constexpr int kRowHeaderWords = 16;
+// Exponent offset of a row tile without nonzero components.
+constexpr int32_t kNoExp = -4000;
 // Column slices a dense diagonal block is cut into (one per row-side warp).
 constexpr int kDenseSlices = 8;
 
+// Digit planes of a width-w code, and whether its top plane is a nibble.
+inline int code_planes(int w) { return (w + 7) / 8; }
+inline bool top_is_nibble(int w) { return w - 8 * (code_planes(w) - 1) <= 4; }
+
 // Byte offsets of each section inside the device arena.
 struct Sections {
-    size_t perm, lr, dd, comp_w, comp_s, tasks, task_comp, qwords, pwords, dense, tiles, items;
+    size_t perm, lr, dd, comp_w, comp_s, tasks, task_rec, qcodes, pcodes, dense, tiles, units, kp_info,
+        slot_comp, kpg_tile, comp_part;
     size_t total;
 };
 
 struct Layout {
     uint64_t order = 0;
-    int32_t n_lr = 0, n_dense = 0, n_comp = 0, n_tiles = 0, n_items = 0, n_chunks = 0;
+    int32_t n_lr = 0, n_dense = 0, n_comp = 0, n_tiles = 0, n_chunks = 0;
     int32_t n_tasks = 0, n_split = 0, max_parts = 1;
+    int32_t n_units = 0, n_slots = 0, n_dense_parts = 0, n_kpg = 0;
     std::vector<uint8_t> arena;  // host image of the device arena
     Sections sec{};
     double bound = 0;
     // traffic model (reference word counts) and stored sizes
     uint64_t code_bytes = 0, left_code_bytes = 0, right_code_bytes = 0, scale_bytes = 0,
              dense_bytes = 0, flops = 0;
-    uint64_t stored_q_words = 0, stored_p_words = 0;
+    uint64_t stored_q_bytes = 0, stored_p_bytes = 0;
 };
 
 Layout build_layout(const HostMatrix& m);

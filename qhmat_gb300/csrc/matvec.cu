@@ -34,6 +34,7 @@
 // |u|), the product s^P s^Q, the alignment of blocks more than 2^16 below the
 // tile's largest, and the final FP64 conversions: the result agrees with the
 // reference's FP64 matmul (src/qhmat/core.cpp:360-390) to ~1e-15 in norm.
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -42,6 +43,8 @@
 #include <cstring>
 #include <mutex>
 #include <new>
+#include <numeric>
+#include <queue>
 #include <string>
 #include <vector>
 
@@ -51,17 +54,11 @@
 namespace qhg {
 namespace {
 
-// Fixed point: |X|, |U| <= 2^kFixBits, split into two kLimb-bit limbs (low
-// limb unsigned, high limb signed).  A code (|c| < 2^31) times a limb is
-// < 2^58, so an int64 accumulator takes kFoldEvery products before it is
-// folded into a wider integer.
-constexpr int kFixBits = 54;
-constexpr int kLimb = 27;
-constexpr long long kLimbMask = (1LL << kLimb) - 1;
-// (kFoldEvery = kColChunk: one column chunk, or 32 row-side components.)
-// Guard bits of the row accumulator: a block whose largest |u| is within
-// 2^kGuard of the tile's largest is added without rounding.
-constexpr int kGuard = 16;
+// Fixed point: x (per rhs column) and u (per row tile) are held as integers
+// X = round(v * 2^(kFixBits - (e - 1022))), |X| <= 2^kFixBits, on one exponent
+// field e; the tensor-core operand is X's eight base-256 limbs (seven unsigned,
+// the top one signed), each an exact f16.
+constexpr int kFixBits = 62;
 
 
 // ---------------------------------------------------------------- helpers
@@ -86,27 +83,16 @@ __device__ __forceinline__ long long to_fixed(double v, int emax) {
     return bits < 0 ? -q : q;
 }
 
-// Sign-extend the low W bits of r.
-template <int W>
-__device__ __forceinline__ int sext(uint32_t r) {
-    return int(r << (32 - W)) >> (32 - W);
+// The eight limbs of X as f16 values (limb k in half k): X = sum_k l_k 2^(8k).
+__device__ __forceinline__ uint4 to_limbs(long long X) {
+    uint32_t h[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const int v = k < 7 ? int((X >> (8 * k)) & 255) : int(X >> 56);
+        h[k] = __half_as_ushort(__int2half_rn(v));
+    }
+    return make_uint4(h[0] | (h[1] << 16), h[2] | (h[3] << 16), h[4] | (h[5] << 16), h[6] | (h[7] << 16));
 }
-
-// Code e of a bit string held in registers w[0..]: bits [e*W, e*W + W),
-// LSB-first -- the field HMatrix::decode reads (core.cpp:269-282).  Called
-// from fully unrolled loops, so the word index and shift are constants.
-template <int W>
-__device__ __forceinline__ int code_at(const uint32_t* w, int e) {
-    const int pos = e * W, wi = pos >> 5, off = pos & 31;
-    if (off + W <= 32) return sext<W>(w[wi] >> off);
-    return sext<W>(__funnelshift_r(w[wi], w[wi + 1], off));
-}
-
-// (hi * 2^kLimb + lo) as a 128-bit integer.
-__device__ __forceinline__ __int128 widen(long long hi, long long lo) {
-    return ((__int128)hi << kLimb) + lo;
-}
-
 
 struct Arena {
     const int32_t* perm;
@@ -115,21 +101,29 @@ struct Arena {
     const uint8_t* comp_w;
     const double* comp_s;
     const ColTask* tasks;
-    const int32_t* task_comp;
-    const uint32_t* qwords;
-    const uint32_t* pwords;
+    const TaskRec* task_rec;
+    const uint8_t* qcodes;
+    const uint8_t* pcodes;
     const double* dense;
     const RowTile* tiles;
-    const RowItem* items;
+    const RowUnit* units;
+    const uint8_t* kp_info;
+    const int32_t* slot_comp;
+    const int32_t* kpg_tile;
+    const int32_t* comp_part;
 };
 
 struct Work {
-    double* xc;        // [rhs][n]  x in clustered order (FP64)
-    int2* xl;          // [rhs][n]  x in fixed point on its column's exponent, two limbs
-    int* xe;           // [rhs]     largest exponent field of x (zeroed before prep_x)
-    int* split_cnt;    // [n_split][rhs] finished parts of each split column task (zeroed)
-    long long* part;   // [n_split][max_parts][rhs][32][2] partial sums of split tasks
-    double* u;         // [rhs][n_comp] u_bj = s^P s^Q t_bj (FP64)
+    double* xc;        // [rhs][n]            x in clustered order (FP64)
+    int* xblk;         // [rhs][nblk]         largest exponent field of x per prep block
+    int* xe;           // [rhs]               largest exponent field of x
+    uint4* xq;         // [rhs][n_pad]        limbs of X (zero past n)
+    long long* lsum;   // [rhs][n_comp][8]    per-limb sums sum_i c_ij limb_l(X_i) of each component
+    long long* lsplit; // [rhs][n_split*32][8] the same for components of split tasks (zeroed by prep)
+    uint4* blimb;      // [rhs][n_slots]      row-side B rows: limbs of U
+    uint4* kpbias;     // [rhs][n_kpg]        sum of 2^(w-1) U over each B row group (128-bit)
+    uint4* plr;        // [rhs][n_tiles][8][16] low-rank row sums of each row unit (128-bit)
+    double* pdense;    // [rhs][n_dense_parts][64] dense slice row sums
 };
 
 // -------------------------------------------------- bulk copies (TMA)
@@ -147,18 +141,23 @@ __device__ __forceinline__ void mbar_arrive_expect(uint64_t* bar, unsigned bytes
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes)
                  : "memory");
 }
+// Potentially blocking test of a phase: the thread is suspended until the
+// phase completes or kSuspendNs nanoseconds pass, so that a waiting warp does
+// not spin on the issue slots the computing warps need.
+constexpr unsigned kSuspendNs = 1000000u;
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
     unsigned ok;
     asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
         : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
+        : "r"(smem_u32(bar)), "r"(parity), "r"(kSuspendNs)
         : "memory");
     return ok != 0;
 }
-// Bounded wait: gives up (returns false) after kWaitLimit polls instead of
-// hanging; callers record the failure in the status word and stop.
-constexpr int kWaitLimit = 1 << 22;
+// Bounded wait: gives up (returns false) after kWaitLimit tests (at most about
+// kWaitLimit * kSuspendNs) instead of hanging; callers record the failure in
+// the status word and stop.
+constexpr int kWaitLimit = 2048;
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
     for (int i = 0; i < kWaitLimit; ++i)
         if (mbar_try_wait(bar, parity)) return true;
@@ -177,13 +176,10 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned b
         : "memory");
 }
 
-// Slot of a warp's prefetch pipeline: up to 4 KB of code words plus up to 33
-// doubles (x entries or u values, copied from an 8-byte-aligned start rounded
-// down to 16 bytes).
-constexpr int kSlotBytes = kStageWordBytes + 272;
 constexpr int kStages = 3;
 constexpr int kWarps = 8;
-constexpr int kPipeSmem = kWarps * kStages * kSlotBytes;
+constexpr int kColPipeSmem = kWarps * kStages * kColSlotBytes;
+constexpr int kRowPipeSmem = kWarps * kStages * kRowSlotBytes;
 
 // Status bits written by the kernels (status word of the apply).
 constexpr int kStatusNonfinite = 1;
@@ -227,213 +223,340 @@ __device__ __forceinline__ double i128_ldexp(__int128 v, int k) {
     return __longlong_as_double((long long)bits);
 }
 
-// ------------------------------------------------------------- decoders
+__device__ __forceinline__ __int128 shfl_xor_i128(__int128 v, int m) {
+    const long long lo = __shfl_xor_sync(0xFFFFFFFFu, (long long)v, m);
+    const long long hi = __shfl_xor_sync(0xFFFFFFFFu, (long long)(v >> 64), m);
+    return ((__int128)hi << 64) | (unsigned long long)lo;
+}
 
-// Column side: the 32 codes of lane `lane`'s chunk `ch` of a task (layout.hpp:
-// word v of the chunk at q[(ch*W + v)*count + lane]).
-template <int W>
-__device__ __forceinline__ void col_chunk_words(const uint32_t* __restrict__ q, int ch, int count, int lane,
-                                                uint32_t (&w)[W]) {
-    const uint32_t* base = q + (size_t)ch * W * count + lane;
+// ------------------------------------------------- tensor-core fragments
+//
+// A digit d enters the MMA as the f16 bit pattern d, i.e. the subnormal
+// d * 2^-24, so a byte or nibble becomes an operand with one permute (bytes)
+// or one shift-and-mask (nibbles); products with the normal-f16 limbs are
+// exact and every accumulator value is an integer times 2^-24 below 1, exact
+// in FP32.
+
+__device__ __forceinline__ uint32_t prmt(uint32_t a, uint32_t b, uint32_t sel) {
+    uint32_t r;
+    asm("prmt.b32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(sel));
+    return r;
+}
+// Byte group word (digits of entries 2t, 2t+1, 2t+8, 2t+9): the f16 pairs of
+// entries (2t, 2t+1) and (2t+8, 2t+9).
+__device__ __forceinline__ uint32_t dig_lo(uint32_t w) { return prmt(w, 0u, 0x4140u); }
+__device__ __forceinline__ uint32_t dig_hi(uint32_t w) { return prmt(w, 0u, 0x4342u); }
+// Nibble group word: pair k = (nibble k, nibble k + 4); k = 0, 1 are k-block
+// 0's pairs (2t, 2t+1) and (2t+8, 2t+9), k = 2, 3 k-block 1's.
+__device__ __forceinline__ uint32_t nib_pair(uint32_t v, int k) { return (v >> (4 * k)) & 0x000F000Fu; }
+
+// d += A * B for one 16x8x16 step (A: rows g, g+8 x k 2t.., 2t+8..).
+__device__ __forceinline__ void mma_dig(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
+                                        uint32_t b0, uint32_t b1) {
+    asm("mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3},{%4,%5,%6,%7},{%8,%9},{%0,%1,%2,%3};"
+                 : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+                 : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+// B fragments of two k-blocks from 32 rows of 16 bytes (limbs of 32 entries
+// or components) at a 16-byte-aligned shared address: lane l points at row l.
+__device__ __forceinline__ void limb_frags(uint32_t row_addr, uint32_t (&b)[4]) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(b[0]), "=r"(b[1]), "=r"(b[2]), "=r"(b[3])
+                 : "r"(row_addr)
+                 : "memory");
+}
+
+// One group (rows g and g+8 of a 16-row fragment pair of k-blocks, in
+// shared memory at grp) into d.  Byte rows are 32 bytes, nibble rows 16; rows
+// >= `rows` are zero.  Plain loads (ordered after the stage's mbarrier wait,
+// which clobbers memory) and non-volatile MMAs leave the compiler free to
+// overlap one group's loads with the previous group's MMAs.
+__device__ __forceinline__ void group_mma(float (&d)[4], const uint8_t* grp, bool nib, int rows, int g, int t,
+                                          const uint32_t (&b)[4]) {
+    if (nib) {
+        const uint32_t v0 = g < rows ? *reinterpret_cast<const uint32_t*>(grp + g * 16 + 4 * t) : 0u;
+        const uint32_t v1 = g + 8 < rows ? *reinterpret_cast<const uint32_t*>(grp + (g + 8) * 16 + 4 * t) : 0u;
+        mma_dig(d, nib_pair(v0, 0), nib_pair(v1, 0), nib_pair(v0, 1), nib_pair(v1, 1), b[0], b[1]);
+        mma_dig(d, nib_pair(v0, 2), nib_pair(v1, 2), nib_pair(v0, 3), nib_pair(v1, 3), b[2], b[3]);
+    } else {
+        const uint2 w0 = g < rows ? *reinterpret_cast<const uint2*>(grp + g * 32 + 8 * t) : make_uint2(0u, 0u);
+        const uint2 w1 =
+            g + 8 < rows ? *reinterpret_cast<const uint2*>(grp + (g + 8) * 32 + 8 * t) : make_uint2(0u, 0u);
+        mma_dig(d, dig_lo(w0.x), dig_lo(w1.x), dig_hi(w0.x), dig_hi(w1.x), b[0], b[1]);
+        mma_dig(d, dig_lo(w0.y), dig_lo(w1.y), dig_hi(w0.y), dig_hi(w1.y), b[2], b[3]);
+    }
+}
+
+// The top plane of a column task: stored digits s = d + 2^(t-1) become the
+// signed digit d as a normal f16 (1024 + s, minus hb = 1024 + 2^(t-1) in both
+// halves), so no offset correction is needed on the column side.
+__device__ __forceinline__ uint32_t hsub2(uint32_t a, uint32_t b) {
+    uint32_t r;
+    asm("sub.f16x2 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b));
+    return r;
+}
+__device__ __forceinline__ uint32_t top_lo(uint32_t w, uint32_t hb) { return hsub2(prmt(w, 0x64646464u, 0x4140u), hb); }
+__device__ __forceinline__ uint32_t top_hi(uint32_t w, uint32_t hb) { return hsub2(prmt(w, 0x64646464u, 0x4342u), hb); }
+__device__ __forceinline__ uint32_t top_nib(uint32_t v, int k, uint32_t hb) {
+    return hsub2(nib_pair(v, k) | 0x64006400u, hb);
+}
+__device__ __forceinline__ void group_mma_top(float (&d)[4], const uint8_t* grp, bool nib, int rows, int g, int t,
+                                              const uint32_t (&b)[4], uint32_t hb) {
+    // rows past `rows` contribute zero: their operands are forced to +0.0
+    const bool in0 = g < rows, in1 = g + 8 < rows;
+    if (nib) {
+        const uint32_t v0 = in0 ? *reinterpret_cast<const uint32_t*>(grp + g * 16 + 4 * t) : 0u;
+        const uint32_t v1 = in1 ? *reinterpret_cast<const uint32_t*>(grp + (g + 8) * 16 + 4 * t) : 0u;
+        uint32_t a[8];
 #pragma unroll
-    for (int v = 0; v < W; ++v) w[v] = __ldg(base + (size_t)v * count);
+        for (int k = 0; k < 4; ++k) {
+            a[k] = in0 ? top_nib(v0, k, hb) : 0u;
+            a[4 + k] = in1 ? top_nib(v1, k, hb) : 0u;
+        }
+        mma_dig(d, a[0], a[4], a[1], a[5], b[0], b[1]);
+        mma_dig(d, a[2], a[6], a[3], a[7], b[2], b[3]);
+    } else {
+        const uint2 w0 = in0 ? *reinterpret_cast<const uint2*>(grp + g * 32 + 8 * t) : make_uint2(0u, 0u);
+        const uint2 w1 = in1 ? *reinterpret_cast<const uint2*>(grp + (g + 8) * 32 + 8 * t) : make_uint2(0u, 0u);
+        const uint32_t a0 = in0 ? top_lo(w0.x, hb) : 0u, a2 = in0 ? top_hi(w0.x, hb) : 0u;
+        const uint32_t a4 = in0 ? top_lo(w0.y, hb) : 0u, a6 = in0 ? top_hi(w0.y, hb) : 0u;
+        const uint32_t a1 = in1 ? top_lo(w1.x, hb) : 0u, a3 = in1 ? top_hi(w1.x, hb) : 0u;
+        const uint32_t a5 = in1 ? top_lo(w1.y, hb) : 0u, a7 = in1 ? top_hi(w1.y, hb) : 0u;
+        mma_dig(d, a0, a1, a2, a3, b[0], b[1]);
+        mma_dig(d, a4, a5, a6, a7, b[2], b[3]);
+    }
 }
 
-template <int W>
-__device__ __forceinline__ void col_chunk_codes(const uint32_t (&w)[W], int (&c)[32]) {
-#pragma unroll
-    for (int e = 0; e < 32; ++e) c[e] = code_at<W>(w, e);
+// Digits of rows g, g+8 of a group as integers, in the order the MMA sees
+// them (for validation): out[half][kb*4 + s], s = entries 2t, 2t+1, 2t+8, 2t+9.
+__device__ __forceinline__ void group_digits(const uint8_t* grp, bool nib, int rows, int g, int t,
+                                             uint32_t (&out)[2][8]) {
+    uint32_t r[2][4];  // [half][kb0 lo, kb0 hi, kb1 lo, kb1 hi]
+    if (nib) {
+        const uint32_t v0 = g < rows ? *reinterpret_cast<const uint32_t*>(grp + g * 16 + 4 * t) : 0u;
+        const uint32_t v1 = g + 8 < rows ? *reinterpret_cast<const uint32_t*>(grp + (g + 8) * 16 + 4 * t) : 0u;
+        for (int k = 0; k < 4; ++k) {
+            r[0][k] = nib_pair(v0, k);
+            r[1][k] = nib_pair(v1, k);
+        }
+    } else {
+        const uint2 w0 = g < rows ? *reinterpret_cast<const uint2*>(grp + g * 32 + 8 * t) : make_uint2(0u, 0u);
+        const uint2 w1 =
+            g + 8 < rows ? *reinterpret_cast<const uint2*>(grp + (g + 8) * 32 + 8 * t) : make_uint2(0u, 0u);
+        r[0][0] = dig_lo(w0.x), r[0][1] = dig_hi(w0.x), r[0][2] = dig_lo(w0.y), r[0][3] = dig_hi(w0.y);
+        r[1][0] = dig_lo(w1.x), r[1][1] = dig_hi(w1.x), r[1][2] = dig_lo(w1.y), r[1][3] = dig_hi(w1.y);
+    }
+    for (int hh = 0; hh < 2; ++hh)
+        for (int k = 0; k < 4; ++k) {
+            // pair k: k-block k >> 1, slots (2(k&1), 2(k&1) + 1)
+            out[hh][(k >> 1) * 4 + 2 * (k & 1)] = r[hh][k] & 0xFFFFu;
+            out[hh][(k >> 1) * 4 + 2 * (k & 1) + 1] = r[hh][k] >> 16;
+        }
+}
+// Entry (within a 32-entry k-pair) of slot s of k-block kb for thread t.
+__device__ __forceinline__ int slot_entry(int kb, int s, int t) { return 16 * kb + 2 * t + (s & 1) + 8 * (s >> 1); }
+
+// Exact integers sum(D * 2^24) of a plane's accumulators, folded into 64-bit
+// sums at weight 2^(8m).
+__device__ __forceinline__ long long fold(float d, int m) {
+    return (long long)__float2int_rn(d * 16777216.0f) << (8 * m);
 }
 
-// Row side: codes of rows 2*lane and 2*lane+1 of a piece (the bit string of
-// the tile's rows of one component, from a fresh word), width W at run time.
-// No branches: three words are read and the shift amounts computed, because a
-// data-dependent branch per component stalls the warp far longer than the
-// extra arithmetic.
-__device__ __forceinline__ void row_pair_codes_rt(const uint32_t* piece, int lane, int W, int& c0, int& c1) {
-    const uint32_t pos = uint32_t(lane) * uint32_t(2 * W);
-    const uint32_t wi = pos >> 5, off = pos & 31;
-    const uint32_t a = piece[wi], b = piece[wi + 1], d = piece[wi + 2];
-    const uint32_t sh = 32u - uint32_t(W);
-    c0 = int(__funnelshift_r(a, b, off) << sh) >> sh;
-    const uint32_t p1 = off + uint32_t(W);
-    const uint32_t lo = p1 < 32 ? a : b, hi = p1 < 32 ? b : d;
-    c1 = int(__funnelshift_r(lo, hi, p1 & 31) << sh) >> sh;
-}
-
-// Dispatch a width to a template instance.
+// Widths a code may have (the reference's writer allows 2..32).
 #define QH_WIDTH_CASES(X) \
     X(2) X(3) X(4) X(5) X(6) X(7) X(8) X(9) X(10) X(11) X(12) X(13) X(14) X(15) X(16) X(17) \
     X(18) X(19) X(20) X(21) X(22) X(23) X(24) X(25) X(26) X(27) X(28) X(29) X(30) X(31) X(32)
 
 // ---------------------------------------------------------------- kernels
 
-// One warp per (chunk of 32 clustered positions, rhs column): clustered FP64
-// copy of x, largest exponent field per column (atomicMax), nonfinite flag.
-__global__ void __launch_bounds__(256) prep_x_kernel(Arena A, Work W, const double* __restrict__ x,
-                                                     int n, int rhs, int n_chunks, int* status) {
-    const int lane = threadIdx.x & 31;
-    const long long gw = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    const long long total = (long long)n_chunks * rhs;
-    if (gw >= total) return;
-    const int p = int(gw / n_chunks), chunk = int(gw % n_chunks);
+__device__ __forceinline__ void st_i128(uint4* p, __int128 v) {
+    *p = make_uint4(uint32_t(v), uint32_t(v >> 32), uint32_t(v >> 64), uint32_t(v >> 96));
+}
+__device__ __forceinline__ __int128 ld_i128(const uint4* p) {
+    const uint4 v = __ldcg(p);
+    return (__int128)(((unsigned __int128)v.w << 96) | ((unsigned __int128)v.z << 64) |
+                      ((unsigned __int128)v.y << 32) | v.x);
+}
+
+// Block (bx, p) of 8 warps: chunks 8bx .. 8bx+7 of rhs column p.  Clustered
+// FP64 copy of x, the block's largest exponent field, nonfinite flag; the
+// grid also zeroes the apply's counters.
+__global__ void __launch_bounds__(256) prep_x_kernel(Arena A, Work W, const double* __restrict__ x, int n, int rhs,
+                                                     int n_chunks, int* zero, int n_zero, int* status) {
+    __shared__ int s_m[8];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int p = blockIdx.y;
+    const int chunk = blockIdx.x * 8 + warp;
     const int pos = chunk * kChunk + lane;
-    const bool valid = pos < n;
+    const bool valid = chunk < n_chunks && pos < n;
     const double v = valid ? __ldg(x + (long long)__ldg(A.perm + pos) * rhs + p) : 0.0;
     const int e = exp_field(v);
     if (__any_sync(0xFFFFFFFFu, e == 0x7FF) && lane == 0 && status) atomicOr(status, kStatusNonfinite);
-    const int emax = __reduce_max_sync(0xFFFFFFFFu, e == 0x7FF ? 0 : e);
+    const int em = __reduce_max_sync(0xFFFFFFFFu, e == 0x7FF ? 0 : e);
     if (valid) W.xc[(long long)p * n + pos] = e == 0x7FF ? 0.0 : v;
-    if (lane == 0 && emax) atomicMax(W.xe + p, emax);
-}
-
-// x in fixed point on its column's exponent (one thread per entry), after
-// prep_x_kernel has found the exponent.
-__global__ void __launch_bounds__(256) x_limbs_kernel(Work W, int n, int rhs) {
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= (long long)n * rhs) return;
-    const int p = int(i / n);
-    const int xe = W.xe[p];
-    const long long X = xe ? to_fixed(W.xc[i], xe) : 0;
-    W.xl[i] = make_int2(int(X & kLimbMask), int(X >> kLimb));
-}
-
-// sum_{e<NE} code_e * X_e for NE codes held in registers w[], decoded as
-// consumed.
-template <int W, int NE>
-__device__ __forceinline__ void codes_mac(const uint32_t* w, const int2* sX, long long& alo, long long& ahi) {
-    // four independent accumulator pairs keep the multiply-add chains short
-    long long l[4] = {0, 0, 0, 0}, h[4] = {0, 0, 0, 0};
-#pragma unroll
-    for (int e = 0; e < NE; ++e) {
-        const int2 xx = sX[e];
-        const int c = code_at<W>(w, e);
-        l[e & 3] += (long long)c * xx.x;
-        h[e & 3] += (long long)c * xx.y;
+    if (lane == 0) s_m[warp] = em;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int m = 0;
+        for (int i = 0; i < 8; ++i) m = max(m, s_m[i]);
+        W.xblk[(long long)p * gridDim.x + blockIdx.x] = m;
     }
-    alo += (l[0] + l[1]) + (l[2] + l[3]);
-    ahi += (h[0] + h[1]) + (h[2] + h[3]);
+    const long long tid = ((long long)blockIdx.y * gridDim.x + blockIdx.x) * blockDim.x + threadIdx.x;
+    const long long nthr = (long long)gridDim.x * gridDim.y * blockDim.x;
+    for (long long i = tid; i < n_zero; i += nthr) zero[i] = 0;
 }
 
-// One 32-entry chunk of a column task from a stage: lane l's words are
-// st.words[v * count + l].  Widths above 16 in two halves of 16 codes.
-template <int W>
-__device__ __forceinline__ void column_chunk(const uint32_t* sw, int count, int lane, const int2* sX,
-                                             long long& alo, long long& ahi) {
-    const uint32_t* base = sw + lane;
-    if constexpr (W <= 16 || (W & 1)) {
-        uint32_t w[W];
-#pragma unroll
-        for (int v = 0; v < W; ++v) w[v] = base[v * count];
-        codes_mac<W, 32>(w, sX, alo, ahi);
-    } else {
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            uint32_t w[W / 2];
-#pragma unroll
-            for (int v = 0; v < W / 2; ++v) w[v] = base[(h * (W / 2) + v) * count];
-            codes_mac<W, 16>(w, sX + 16 * h, alo, ahi);
-        }
-    }
+// Block (bx, p): the column's exponent from the prep blocks' maxima, then the
+// limbs of X for 256 entries (zero past n).
+__global__ void __launch_bounds__(256) x_limbs_kernel(Work W, int n, int n_pad, int nblk) {
+    __shared__ int s_m[8];
+    const int p = blockIdx.y, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int m = 0;
+    for (int i = threadIdx.x; i < nblk; i += blockDim.x) m = max(m, W.xblk[(long long)p * nblk + i]);
+    m = __reduce_max_sync(0xFFFFFFFFu, m);
+    if (lane == 0) s_m[warp] = m;
+    __syncthreads();
+    int xe = 0;
+    for (int i = 0; i < 8; ++i) xe = max(xe, s_m[i]);
+    if (blockIdx.x == 0 && threadIdx.x == 0) W.xe[p] = xe;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n_pad) return;
+    const long long X = (k < n && xe) ? to_fixed(W.xc[(long long)p * n + k], xe) : 0;
+    W.xq[(long long)p * n_pad + k] = to_limbs(X);
 }
 
-__device__ __noinline__ void column_chunk_any(const uint32_t* sw, int W, int count, int lane, const int2* sX,
-                                              long long* a2) {
-    long long alo = 0, ahi = 0;
-    for (int e = 0; e < 32; ++e) {
-        const int pos = e * W, wi = pos >> 5, off = pos & 31;
-        const uint32_t lo = sw[wi * count + lane];
-        const uint32_t hi = off + W > 32 ? sw[(wi + 1) * count + lane] : 0u;
-        const uint32_t r = __funnelshift_r(lo, hi, off);
-        const int c = W == 32 ? int(r) : (int(r << (32 - W)) >> (32 - W));
-        const int2 xx = sX[e];
-        alo += (long long)c * xx.x;
-        ahi += (long long)c * xx.y;
-    }
-    a2[0] = alo;
-    a2[1] = ahi;
+// Bring a line into L1 ahead of its use (no register waits on it).
+__device__ __forceinline__ void prefetch_l1(const void* p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
+
+// A column unit's descriptor (four 16-byte loads, cached in L1).
+__device__ __forceinline__ ColTask load_task(const ColTask* p) {
+    const int4* q = reinterpret_cast<const int4*>(p);
+    const int4 a = __ldg(q), b = __ldg(q + 1), c = __ldg(q + 2), d = __ldg(q + 3);
+    ColTask T;
+    T.col0 = a.x, T.n = a.y, T.count = a.z, T.width = a.w;
+    T.off = (long long)(((unsigned long long)(unsigned)b.y << 32) | (unsigned)b.x);
+    T.stride = b.z, T.comp_idx = b.w;
+    T.chunk0 = c.x, T.nchunks = c.y, T.part = c.z, T.nparts = c.w;
+    T.split_id = d.x, T.cps = d.y;
+    return T;
 }
 
-// Descriptor fields of one column unit, kept one per lane.
-struct ColDesc {
-    long long word0;
-    int col0, n, width, count, stride, comp_idx, chunk0, nchunks, part, nparts, split_id;
+// Column-side accumulators of one warp: FP32 MMA sums per M-tile and plane
+// (exact below 2^24), their 64-bit folds, and the same for sum_i X_i.
+struct ColAcc {
+    float D[2][4][4];
+    long long acc[2][4];
+    int since;
 };
 
-__device__ __forceinline__ ColDesc shfl_desc(const ColDesc& d, int src) {
-    ColDesc r;
-    r.word0 = __shfl_sync(0xFFFFFFFFu, d.word0, src);
-    r.col0 = __shfl_sync(0xFFFFFFFFu, d.col0, src);
-    r.n = __shfl_sync(0xFFFFFFFFu, d.n, src);
-    r.width = __shfl_sync(0xFFFFFFFFu, d.width, src);
-    r.count = __shfl_sync(0xFFFFFFFFu, d.count, src);
-    r.stride = __shfl_sync(0xFFFFFFFFu, d.stride, src);
-    r.comp_idx = __shfl_sync(0xFFFFFFFFu, d.comp_idx, src);
-    r.chunk0 = __shfl_sync(0xFFFFFFFFu, d.chunk0, src);
-    r.nchunks = __shfl_sync(0xFFFFFFFFu, d.nchunks, src);
-    r.part = __shfl_sync(0xFFFFFFFFu, d.part, src);
-    r.nparts = __shfl_sync(0xFFFFFFFFu, d.nparts, src);
-    r.split_id = __shfl_sync(0xFFFFFFFFu, d.split_id, src);
-    return r;
+// Fold the FP32 sums into the 64-bit per-limb sums: plane m < P-1 holds
+// subnormal digits (sums in units of 2^-24), the top plane signed digits
+// (units of 1); plane m weighs 2^(8m).
+template <int P>
+__device__ __forceinline__ void col_fold(ColAcc& a) {
+#pragma unroll
+    for (int q = 0; q < 2; ++q)
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            long long v = 0;
+#pragma unroll
+            for (int m = 0; m < P; ++m) {
+                const float d = m == P - 1 ? a.D[q][m][r] : a.D[q][m][r] * 16777216.0f;
+                v += (long long)__float2int_rn(d) << (8 * m);
+                a.D[q][m][r] = 0.f;
+            }
+            a.acc[q][r] += v;
+        }
+    a.since = 0;
 }
 
-// Chunks of one (unit, column) that one pipeline step carries: as many as fit
-// a slot (code words plus 32 x entries per chunk), at least one.
-__device__ __forceinline__ int col_step_chunks(int stride, int remaining) {
-    const int per = stride * 4 + kColChunk * 8;
-    return max(1, min(remaining, (kSlotBytes - 16) / per));
+// The chunks of a step of a task with P planes (nibble top plane if nibtop):
+// per chunk, the x limbs' B fragments and two MMAs per (M-tile, plane) group.
+template <int P>
+__device__ __forceinline__ void col_step(ColAcc& a, const uint8_t* slot, int nc, int stride, int count, bool nibtop,
+                                         uint32_t hb, int g, int t, int lane) {
+    const int RB = (P - 1) * 32 + (nibtop ? 16 : 32);  // bytes of one row over all planes
+    const uint32_t xrow = smem_u32(slot + nc * stride) + 16u * unsigned(lane);
+    const int rows0 = count < 16 ? count : 16, rows1 = count - 16;
+    for (int c = 0; c < nc; ++c) {
+        const uint8_t* cb = slot + c * stride;
+        uint32_t b[4];
+        limb_frags(xrow + unsigned(c * kColChunk * 16), b);
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            const int rows = q ? rows1 : rows0;
+            if (rows <= 0) break;
+            const uint8_t* off = cb + q * 16 * RB;
+#pragma unroll
+            for (int m = 0; m < P - 1; ++m) {
+                group_mma(a.D[q][m], off, false, rows, g, t, b);
+                off += rows * 32;
+            }
+            group_mma_top(a.D[q][P - 1], off, nibtop, rows, g, t, b, hb);
+        }
+        if (++a.since == 8) col_fold<P>(a);
+    }
 }
 
-// Column side.  Warp gw owns units gw, gw + G, ... (heaviest first); its work
+// Column side.  Warp gw owns the units warp_off[gw] .. warp_off[gw + 1]
+// (assigned longest first at upload, heaviest first per warp); its work
 // is the sequence (unit, rhs column, chunk), streamed through a kStages-deep
-// pipeline of shared-memory slots filled by bulk copies (one per step for the
-// code words, one for the x entries), kStages - 1 steps ahead of their use;
-// a step carries as many chunks as fit a slot.  Lane l accumulates component
-// l of the unit exactly; a unit's last chunk converts the sum (or, for a
-// split task, hands it to the part that finishes last).
-__global__ void __launch_bounds__(kWarps * 32, 2) column_kernel(Arena A, Work W, int n_tasks, int n, int rhs,
-                                                                int n_comp, int max_parts, int* status) {
+// pipeline of shared-memory slots filled by bulk copies (the chunks' code
+// groups and the limbs of their x entries), kStages - 1 steps ahead of their
+// use.  Per chunk the warp runs, for each M-tile and digit plane, two
+// 16x8x16 MMAs (digits x the eight x limbs), plus two with an all-ones A for
+// sum_i X_i (the offset-code correction); the FP32 sums are folded into 64-bit
+// integers every 8 chunks (before any can reach 2^24).  At the unit's end the
+// limbs and planes are combined into exact 128-bit sums t_j = sum_i c_ij X_i,
+// and lane (g, t) converts component 16(t>>1) + 8(t&1) + g to
+// u_j = (s^P s^Q) t_j 2^(xe - 1022 - kFixBits).
+__global__ void __launch_bounds__(kWarps * 32, 2) column_kernel(Arena A, Work W, const int* __restrict__ warp_off,
+                                                                int n_pad, int rhs, int n_comp, int n_split,
+                                                                int* status) {
     extern __shared__ __align__(16) uint8_t smem_raw[];
     __shared__ __align__(8) uint64_t s_bar[kWarps][kStages];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint8_t* slots = smem_raw + (size_t)warp * kStages * kSlotBytes;
+    const int g = lane >> 2, t = lane & 3;
+    uint8_t* slots = smem_raw + (size_t)warp * kStages * kColSlotBytes;
     uint64_t* bar = s_bar[warp];
     if (lane == 0) {
         for (int i = 0; i < kStages; ++i) mbar_init(bar + i, 1);
         mbar_init_fence();
     }
     __syncwarp();
-    const int G = gridDim.x * kWarps;
     const int gw = blockIdx.x * kWarps + warp;
-    const int my_units = gw < n_tasks ? (n_tasks - gw + G - 1) / G : 0;
+    const int u0 = __ldg(warp_off + gw), my_units = __ldg(warp_off + gw + 1) - u0;
+    const ColTask* my_tasks = A.tasks + u0;
     unsigned issued = 0, computed = 0;  // running step counters (slot, phase)
     bool failed = false;
-    for (int b0 = 0; b0 < my_units && !failed; b0 += 32) {
-        const int nb = min(32, my_units - b0);
-        ColDesc mine{};
-        if (lane < nb) {
-            const ColTask T = A.tasks[gw + (b0 + lane) * G];
-            mine = {T.word0, T.col0, T.n, T.width, T.count, T.stride, T.comp_idx, T.chunk0, T.nchunks,
-                    T.part, T.nparts, T.split_id};
-        }
+    ColAcc a;
+#pragma unroll
+    for (int q = 0; q < 2; ++q)
+#pragma unroll
+        for (int m = 0; m < 4; ++m)
+#pragma unroll
+            for (int r = 0; r < 4; ++r) a.D[q][m][r] = 0.f;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) a.acc[0][r] = a.acc[1][r] = 0;
+    a.since = 0;
+    if (my_units > 0) {
+        const int nb = my_units;
         int ik = 0, ip = 0, ic = 0;  // issue cursor
-        ColDesc di = shfl_desc(mine, 0);
+        ColTask di = load_task(my_tasks);
         auto issue = [&]() {
             if (ik >= nb) return;
-            const int nc = col_step_chunks(di.stride, di.nchunks - ic);
+            const int nc = min(di.cps, di.nchunks - ic);
             const unsigned slot_i = issued % kStages;
-            uint8_t* slot = slots + slot_i * kSlotBytes;
-            const unsigned wbytes = unsigned(nc * di.stride * 4);
-            const int k0 = (di.chunk0 + ic) * kColChunk;
-            const int cnt = min(di.n - k0, nc * kColChunk);
-            const int2* xa = W.xl + (long long)ip * n + di.col0 + k0;
-            const int xs = int((reinterpret_cast<uintptr_t>(xa) >> 3) & 1);
-            const unsigned xbytes = unsigned(((cnt + xs) * 8 + 15) & ~15);
+            uint8_t* slot = slots + slot_i * kColSlotBytes;
+            const unsigned wbytes = unsigned(nc * di.stride);
+            const unsigned xbytes = unsigned(nc * kColChunk * 16);
+            const long long k0 = (long long)(di.chunk0 + ic) * kColChunk;
             if (lane == 0) {
                 fence_async_smem();
                 mbar_arrive_expect(bar + slot_i, wbytes + xbytes);
-                bulk_load(slot, A.qwords + di.word0 + (long long)(di.chunk0 + ic) * di.stride, wbytes, bar + slot_i);
-                bulk_load(slot + wbytes, xa - xs, xbytes, bar + slot_i);
+                bulk_load(slot, A.qcodes + di.off + (long long)(di.chunk0 + ic) * di.stride, wbytes, bar + slot_i);
+                bulk_load(slot + wbytes, W.xq + (long long)ip * n_pad + di.col0 + k0, xbytes, bar + slot_i);
             }
             ++issued;
             ic += nc;
@@ -441,20 +564,32 @@ __global__ void __launch_bounds__(kWarps * 32, 2) column_kernel(Arena A, Work W,
                 ic = 0;
                 if (++ip == rhs) {
                     ip = 0;
-                    if (++ik < nb) di = shfl_desc(mine, ik);
+                    if (++ik < nb) {
+                        di = load_task(my_tasks + ik);
+                        if (ik + 2 < nb && lane == 0) prefetch_l1(my_tasks + ik + 2);
+                    }
                 }
             }
         };
+        if (lane < 2 && lane + 1 < nb) prefetch_l1(my_tasks + lane + 1);
         __syncwarp();
 #pragma unroll 1
         for (int s = 0; s < kStages - 1; ++s) issue();
         int ck = 0, cp = 0, cc = 0;  // compute cursor
-        ColDesc dc = shfl_desc(mine, 0);
-        __int128 acc = 0;
-        int xe = W.xe[0];
-        // finalize operands, loaded as soon as a unit starts
-        int comp_id = lane < dc.count ? __ldg(A.task_comp + dc.comp_idx + lane) : 0;
-        double comp_sc = lane < dc.count ? __ldg(A.comp_s + comp_id) : 0.0;
+        ColTask dc = di;
+        // components of this lane's rows (16q + g + 8h), loaded as soon as a
+        // unit starts (used at its end)
+        int rc[2][2];
+        auto load_rows = [&]() {
+#pragma unroll
+            for (int q = 0; q < 2; ++q)
+#pragma unroll
+                for (int hh = 0; hh < 2; ++hh) {
+                    const int row = 16 * q + 8 * hh + g;
+                    rc[q][hh] = row < dc.count ? __ldg(&A.task_rec[dc.comp_idx + row].comp) : -1;
+                }
+        };
+        load_rows();
         while (ck < nb) {
             issue();
             const unsigned slot_i = computed % kStages;
@@ -463,78 +598,57 @@ __global__ void __launch_bounds__(kWarps * 32, 2) column_kernel(Arena A, Work W,
                 failed = true;
                 break;
             }
-            const int nc = col_step_chunks(dc.stride, dc.nchunks - cc);
-            const uint8_t* slot = slots + slot_i * kSlotBytes;
-            const uint32_t* sw = reinterpret_cast<const uint32_t*>(slot);
-            const int2* xa = W.xl + (long long)cp * n + dc.col0 + (dc.chunk0 + cc) * kColChunk;
-            const int xs = int((reinterpret_cast<uintptr_t>(xa) >> 3) & 1);
-            const int2* sxs = reinterpret_cast<const int2*>(slot + nc * dc.stride * 4) + xs;
-            for (int c = 0; c < nc; ++c) {
-                // x limbs of the chunk's entries (entries past the range meet
-                // zero codes)
-                const int2* sX = sxs + c * kColChunk;
-                if (lane < dc.count) {
-                    const uint32_t* cw = sw + c * dc.stride;
-                    long long alo = 0, ahi = 0;
-                    switch (dc.width) {
-                        case 4: column_chunk<4>(cw, dc.count, lane, sX, alo, ahi); break;
-                        case 8: column_chunk<8>(cw, dc.count, lane, sX, alo, ahi); break;
-                        case 12: column_chunk<12>(cw, dc.count, lane, sX, alo, ahi); break;
-                        case 16: column_chunk<16>(cw, dc.count, lane, sX, alo, ahi); break;
-                        case 24: column_chunk<24>(cw, dc.count, lane, sX, alo, ahi); break;
-                        case 32: column_chunk<32>(cw, dc.count, lane, sX, alo, ahi); break;
-                        default: {
-                            long long a2[2];
-                            column_chunk_any(cw, dc.width, dc.count, lane, sX, a2);
-                            alo = a2[0];
-                            ahi = a2[1];
-                        }
-                    }
-                    acc += widen(ahi, alo);
-                }
+            const int nc = min(dc.cps, dc.nchunks - cc);
+            const uint8_t* slot = slots + slot_i * kColSlotBytes;
+            const int P = (dc.width + 7) >> 3;
+            const int tb = dc.width - 8 * (P - 1);  // bits of the top digit
+            const bool nibtop = tb <= 4;
+            const uint32_t hb = (0x6400u | (1u << (tb - 1))) * 0x00010001u;
+            switch (P) {
+                case 1: col_step<1>(a, slot, nc, dc.stride, dc.count, nibtop, hb, g, t, lane); break;
+                case 2: col_step<2>(a, slot, nc, dc.stride, dc.count, nibtop, hb, g, t, lane); break;
+                case 3: col_step<3>(a, slot, nc, dc.stride, dc.count, nibtop, hb, g, t, lane); break;
+                default: col_step<4>(a, slot, nc, dc.stride, dc.count, nibtop, hb, g, t, lane); break;
             }
             ++computed;
             cc += nc;
             if (cc == dc.nchunks) {
-                // finished (unit ck, column cp); x ~= X * 2^(xe - 1022 - kFixBits)
-                if (dc.nparts == 1) {
-                    if (lane < dc.count)
-                        W.u[(long long)cp * n_comp + comp_id] = xe ? i128_ldexp(acc, xe - 1022 - kFixBits) * comp_sc : 0.0;
-                } else {
-                    long long* part = W.part + (((long long)dc.split_id * max_parts + dc.part) * rhs + cp) * 64;
-                    part[2 * lane] = (long long)acc;
-                    part[2 * lane + 1] = (long long)(acc >> 64);
-                    __threadfence();
-                    __syncwarp();
-                    int done = 0;
-                    if (lane == 0) done = atomicAdd(W.split_cnt + (long long)dc.split_id * rhs + cp, 1);
-                    done = __shfl_sync(0xFFFFFFFFu, done, 0);
-                    if (done == dc.nparts - 1) {
-                        __threadfence();
-                        __int128 tot = 0;
-                        for (int q = 0; q < dc.nparts; ++q) {
-                            const long long* pq =
-                                W.part + (((long long)dc.split_id * max_parts + q) * rhs + cp) * 64;
-                            const unsigned long long lo = __ldcg((const unsigned long long*)pq + 2 * lane);
-                            const long long hi = __ldcg(pq + 2 * lane + 1);
-                            tot += ((__int128)hi << 64) | lo;
-                        }
-                        if (lane < dc.count)
-                            W.u[(long long)cp * n_comp + comp_id] =
-                                xe ? i128_ldexp(tot, xe - 1022 - kFixBits) * comp_sc : 0.0;
-                    }
+                switch ((dc.width + 7) >> 3) {
+                    case 1: col_fold<1>(a); break;
+                    case 2: col_fold<2>(a); break;
+                    case 3: col_fold<3>(a); break;
+                    default: col_fold<4>(a); break;
                 }
-                acc = 0;
+                // this lane's per-limb sums: rows 16q + g + 8h, limbs 2t, 2t+1
+                // (finished (unit ck, column cp); parts of a split task add
+                // theirs exactly with integer atomics)
+#pragma unroll
+                for (int q = 0; q < 2; ++q)
+#pragma unroll
+                    for (int hh = 0; hh < 2; ++hh) {
+                        const long long l0 = a.acc[q][2 * hh], l1 = a.acc[q][2 * hh + 1];
+                        a.acc[q][2 * hh] = a.acc[q][2 * hh + 1] = 0;
+                        const int c = rc[q][hh];
+                        if (c < 0) continue;
+                        if (dc.nparts == 1) {
+                            long long* dst = W.lsum + ((long long)cp * n_comp + c) * 8 + 2 * t;
+                            *reinterpret_cast<longlong2*>(dst) = make_longlong2(l0, l1);
+                        } else {
+                            const int row = 16 * q + 8 * hh + g;
+                            unsigned long long* dst = reinterpret_cast<unsigned long long*>(
+                                W.lsplit + ((long long)cp * n_split * 32 + dc.split_id * 32 + row) * 8 + 2 * t);
+                            atomicAdd(dst, (unsigned long long)l0);
+                            atomicAdd(dst + 1, (unsigned long long)l1);
+                        }
+                    }
                 cc = 0;
                 if (++cp == rhs) {
                     cp = 0;
                     if (++ck < nb) {
-                        dc = shfl_desc(mine, ck);
-                        comp_id = lane < dc.count ? __ldg(A.task_comp + dc.comp_idx + lane) : 0;
-                        comp_sc = lane < dc.count ? __ldg(A.comp_s + comp_id) : 0.0;
+                        dc = load_task(my_tasks + ck);
+                        load_rows();
                     }
                 }
-                xe = W.xe[cp];
             }
             __syncwarp();
         }
@@ -546,269 +660,300 @@ __global__ void __launch_bounds__(kWarps * 32, 2) column_kernel(Arena A, Work W,
     }
 }
 
-// acc (on exponent e_acc, kGuard guard bits) += v (on exponent ev); the
-// accumulator's exponent rises to ev first if ev is larger.
-__device__ __forceinline__ void add_aligned(__int128& acc0, __int128& acc1, int& e_acc, __int128 v0, __int128 v1,
-                                            int ev) {
-    if (ev > e_acc) {
-        const int d = ev - e_acc;
-        if (d >= 127) {
-            acc0 = acc1 = 0;
-        } else {
-            const __int128 half = (__int128)1 << (d - 1);
-            acc0 = (acc0 + half) >> d;
-            acc1 = (acc1 + half) >> d;
-        }
-        e_acc = ev;
-    }
-    const int sh = (e_acc - ev) - kGuard;
-    if (sh <= 0) {
-        acc0 += v0 << (-sh);
-        acc1 += v1 << (-sh);
-    } else if (sh < 127) {
-        const __int128 half = (__int128)1 << (sh - 1);
-        acc0 += (v0 + half) >> sh;
-        acc1 += (v1 + half) >> sh;
-    }
+// Bytes of a row k-pair's digit groups (kp_info: planes | nibble planes << 3).
+__device__ __forceinline__ int kp_bytes(int info) {
+    const int planes = info & 7, nibs = info >> 3;
+    return planes * 512 - __popc(nibs) * 256;
 }
 
+// B rows of the row side: one warp per group of 32 slots (one k-pair of a
+// row unit).  Lane l forms u of the slot's component from its per-limb sums,
+// puts it in fixed point on the tile's exponent and stores its limbs; the
+// group's offset correction sum 2^(w-1) U is reduced over the warp.
+__global__ void __launch_bounds__(256) expand_kernel(Arena A, Work W, int n_kpg, int n_slots, int n_comp,
+                                                     int n_split, int rhs) {
+    const int lane = threadIdx.x & 31;
+    const long long gw = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (gw >= (long long)n_kpg * rhs) return;
+    const int p = int(gw / n_kpg), kpg = int(gw % n_kpg);
+    const int slot = kpg * 32 + lane;
+    const int c = __ldg(A.slot_comp + slot);
+    const int ce = __ldg(&A.tiles[__ldg(A.kpg_tile + kpg)].c_exp);
+    const int xe = W.xe[p];
+    long long U = 0;
+    int w = 1;
+    if (c >= 0) {
+        // t_c = sum_l 2^(8l) (per-limb sums), exactly; u = (s^P s^Q) t 2^(xe - 1022 - kFixBits)
+        const int pr = __ldg(A.comp_part + c);
+        const long long* ls = pr >= 0 ? W.lsplit + ((long long)p * n_split * 32 + pr) * 8
+                                      : W.lsum + ((long long)p * n_comp + c) * 8;
+        __int128 S = 0;
+#pragma unroll
+        for (int l = 0; l < 8; ++l) S += (__int128)__ldcg(ls + l) << (8 * l);
+        const double uv = xe ? i128_ldexp(S, xe - 1022 - kFixBits) * __ldg(A.comp_s + c) : 0.0;
+        w = __ldg(A.comp_w + c);
+        if (uv != 0.0) U = to_fixed(uv, xe + ce);
+    }
+    W.blimb[(long long)p * n_slots + slot] = to_limbs(U);
+    __int128 b = (__int128)U << (w - 1);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) b += shfl_xor_i128(b, o);
+    if (lane == 0) st_i128(W.kpbias + (long long)p * n_kpg + kpg, b);
+}
+
+// The low-rank fields of a row unit's descriptor (cached in L1).
 struct RowDesc {
-    int block, rloc0, comp, count, words;
-    long long off;
+    long long code_off, kp_off;
+    int tile, kind, q, h, H, nkps, K, slot0;
 };
 
-// Row side: one CTA of kWarps warps per row tile; warp w owns the tile's
-// units w, w + kWarps, ...; lane l owns tile rows 2l and 2l + 1.  Each warp
-// streams its units (for every rhs column) through a kStages-deep cp.async
-// pipeline (a unit's data block and its components' u values).  A unit's
-// u are put in fixed point on the unit's own exponent, its row sums are exact,
-// and they are added into 128-bit row accumulators kept on a running exponent
-// with kGuard guard bits.  Dense diagonal units use FP64 loads directly.
-// Warps combine per rhs column in shared memory in a fixed order.
-__global__ void __launch_bounds__(kWarps * 32, 2) row_kernel(Arena A, Work W, double* __restrict__ y,
-                                                             int n, int rhs, int n_comp, int* status) {
+__device__ __forceinline__ RowDesc load_rdesc(const RowUnit* p) {
+    const int4* q = reinterpret_cast<const int4*>(p);
+    const int4 a = __ldg(q), b = __ldg(q + 1), c = __ldg(q + 2);
+    RowDesc d;
+    d.tile = a.x, d.kind = a.y, d.q = a.z, d.h = a.w;
+    d.H = b.x, d.nkps = b.y, d.K = b.z, d.slot0 = b.w;
+    d.code_off = (long long)(((unsigned long long)(unsigned)c.y << 32) | (unsigned)c.x);
+    d.kp_off = (long long)(((unsigned long long)(unsigned)c.w << 32) | (unsigned)c.z);
+    return d;
+}
+
+// k-pairs [i0, i0 + c) of a row unit that one step carries (digit groups and
+// limb rows), at least one; info_l = this lane's k-pair info (k-pair
+// i0 + lane of the unit's sequence, as loaded for the unit's first 32).
+__device__ __forceinline__ int row_step_kps(int info_l, int nkps, int i0, int base, int& code_bytes) {
+    int bytes = 0, c = 0;
+    code_bytes = 0;
+    while (i0 + c < nkps && c < 32 - (i0 - base)) {
+        const int cb = kp_bytes(__shfl_sync(0xFFFFFFFFu, info_l, i0 - base + c));
+        if (c && bytes + cb + 512 > kRowSlotBytes) break;
+        bytes += cb + 512;
+        code_bytes += cb;
+        ++c;
+    }
+    return c;
+}
+
+// Row side.  Warp gw owns the units warp_off[gw] .. warp_off[gw + 1]
+// (assigned longest first at upload).  A
+// low-rank unit (rows 16q.. of a tile, k-pairs h, h + H, ...) streams its
+// digit groups and B rows through a kStages-deep bulk-copy pipeline; per
+// k-pair it runs, for each plane, two 16x8x16 MMAs of its 16 rows of digits by
+// the components' U limbs, folding the FP32 sums into 64-bit integers every 8
+// k-pairs (at most 16 k-blocks, below 2^24).  At the end the limbs and planes
+// of each row are combined into an exact 128-bit sum and stored as the unit's
+// partial.  A dense unit (a column slice of a dense diagonal block) computes
+// its rows in FP64.  combine_kernel adds the partials.
+__global__ void __launch_bounds__(kWarps * 32, 2) row_kernel(Arena A, Work W, const int* __restrict__ warp_off,
+                                                             int n, int rhs, int n_slots, int n_tiles,
+                                                             int n_dense_parts, int* status) {
     extern __shared__ __align__(16) uint8_t smem_raw[];
     __shared__ __align__(8) uint64_t s_bar[kWarps][kStages];
-    __shared__ int s_e[kWarps];
-    __shared__ double s_diag[kDenseSlices][kTileRows];
-    __shared__ int s_nslices;
-    __shared__ __align__(16) int4 s_tab[kWarps][32];
-    const RowTile T = A.tiles[blockIdx.x];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint8_t* slots = smem_raw + (size_t)warp * kStages * kSlotBytes;
+    const int g = lane >> 2, t = lane & 3;
+    uint8_t* slots = smem_raw + (size_t)warp * kStages * kRowSlotBytes;
     uint64_t* bar = s_bar[warp];
-    const int r0 = 2 * lane, r1 = 2 * lane + 1;
-    const int nunits = T.item1 - T.item0;
-    const int my = warp < nunits ? (nunits - warp + kWarps - 1) / kWarps : 0;
-    if (threadIdx.x == 0) s_nslices = 0;
     if (lane == 0) {
         for (int i = 0; i < kStages; ++i) mbar_init(bar + i, 1);
         mbar_init_fence();
     }
-    __syncthreads();
-    unsigned issued = 0, computed = 0;  // running step counters (slot, phase)
+    __syncwarp();
+    const int gw = blockIdx.x * kWarps + warp;
+    const int u0 = __ldg(warp_off + gw), my_units = __ldg(warp_off + gw + 1) - u0;
+    const RowUnit* my_units_p = A.units + u0;
+    unsigned issued = 0, computed = 0;
     bool failed = false;
-    // A warp's units, one descriptor per lane, in batches of 32; pipeline
-    // steps carry as many consecutive units as fit a slot.
-    for (int p = 0; p < rhs; ++p) {
-        __int128 acc0 = 0, acc1 = 0;
-        int e_acc = 0;
-        for (int b0 = 0; b0 < my && !failed; b0 += 32) {
-            const int nb = min(32, my - b0);
-            RowDesc mine{};
-            if (lane < nb) {
-                const RowItem I = A.items[T.item0 + warp + (b0 + lane) * kWarps];
-                mine = {I.block, I.rloc0, I.comp, I.count, I.words, I.off};
-            }
-            auto desc = [&](int k) {
-                RowDesc d;
-                d.block = __shfl_sync(0xFFFFFFFFu, mine.block, k);
-                d.rloc0 = __shfl_sync(0xFFFFFFFFu, mine.rloc0, k);
-                d.comp = __shfl_sync(0xFFFFFFFFu, mine.comp, k);
-                d.count = __shfl_sync(0xFFFFFFFFu, mine.count, k);
-                d.words = __shfl_sync(0xFFFFFFFFu, mine.words, k);
-                d.off = __shfl_sync(0xFFFFFFFFu, mine.off, k);
-                return d;
-            };
-            // bytes a unit occupies in a slot (words, then its u values copied
-            // from an 8-byte-aligned start rounded down to 16 bytes)
-            const int my_bytes =
-                (lane < nb && mine.block >= 0) ? mine.words * 4 + ((mine.count + 1) * 8 + 15) / 16 * 16 : 0;
-            auto group = [&](int k) {  // units [k, k + m) of one step
-                int m = 1, tot = __shfl_sync(0xFFFFFFFFu, my_bytes, k);
-                while (k + m < nb) {
-                    const int b = __shfl_sync(0xFFFFFFFFu, my_bytes, k + m);
-                    if (tot + b > kSlotBytes) break;
-                    tot += b;
-                    ++m;
-                }
-                return m;
-            };
-            int ik = 0;
-            auto issue = [&]() {
-                if (ik >= nb) return;
-                const int m = group(ik);
-                const unsigned slot_i = issued % kStages;
-                uint8_t* slot = slots + slot_i * kSlotBytes;
-                // total bytes of the step, then the copies (lane 0)
-                unsigned total = 0;
-                for (int q = 0; q < m; ++q) total += unsigned(__shfl_sync(0xFFFFFFFFu, my_bytes, ik + q));
-                if (lane == 0) {
-                    fence_async_smem();
-                    mbar_arrive_expect(bar + slot_i, total);
-                }
-                int off = 0;
-                for (int q = 0; q < m; ++q) {
-                    const RowDesc d = desc(ik + q);
-                    if (d.block < 0) continue;
-                    const double* ua = W.u + (long long)p * n_comp + d.comp;
-                    const int us = int((reinterpret_cast<uintptr_t>(ua) >> 3) & 1);
-                    const unsigned ubytes = unsigned(((d.count + 1) * 8 + 15) / 16 * 16);
-                    if (lane == 0) {
-                        bulk_load(slot + off, A.pwords + d.off, unsigned(d.words * 4), bar + slot_i);
-                        bulk_load(slot + off + d.words * 4, ua - us, ubytes, bar + slot_i);
+    if (my_units > 0) {
+        const int nb = my_units;
+        // issue cursor: unit ik, rhs column ip, k-pair index ii (byte offset
+        // ioff); k-pair infos of the unit's k-pairs ibase .. ibase + 31, one per lane
+        int ik = 0, ip = 0, ii = 0, ibase = 0, iinfo = 0;
+        long long ioff = 0;
+        RowDesc di = load_rdesc(my_units_p);
+        if (lane < 2 && lane + 1 < nb) prefetch_l1(my_units_p + lane + 1);
+        auto load_info = [&](const RowDesc& d, int base) {
+            return (d.kind == 0 && base + lane < d.nkps) ? int(__ldg(A.kp_info + d.kp_off + d.h + (base + lane) * d.H)) : 0;
+        };
+        if (di.kind == 0) iinfo = load_info(di, 0);
+        auto issue = [&]() {
+            while (ik < nb && di.kind != 0) {  // dense units use no slots
+                if (++ip == rhs) {
+                    ip = 0;
+                    if (++ik < nb) {
+                        di = load_rdesc(my_units_p + ik);
+                        if (ik + 2 < nb && lane == 0) prefetch_l1(my_units_p + ik + 2);
+                        ibase = 0;
+                        iinfo = load_info(di, 0);
                     }
-                    off += d.words * 4 + int(ubytes);
                 }
-                ++issued;
-                ik += m;
-            };
-            __syncwarp();
+            }
+            if (ik >= nb) return;
+            if (ii - ibase == 32) {
+                ibase = ii;
+                iinfo = load_info(di, ibase);
+            }
+            int cbytes;
+            const int c = row_step_kps(iinfo, di.nkps, ii, ibase, cbytes);
+            const unsigned slot_i = issued % kStages;
+            uint8_t* slot = slots + slot_i * kRowSlotBytes;
+            const unsigned lbytes = unsigned(c * 512);
+            if (lane == 0) {
+                fence_async_smem();
+                mbar_arrive_expect(bar + slot_i, unsigned(cbytes) + lbytes);
+                bulk_load(slot, A.pcodes + di.code_off + ioff, unsigned(cbytes), bar + slot_i);
+                bulk_load(slot + cbytes, W.blimb + (long long)ip * n_slots + di.slot0 + 32 * ii, lbytes, bar + slot_i);
+            }
+            ++issued;
+            ii += c;
+            ioff += cbytes;
+            if (ii == di.nkps) {
+                ii = 0;
+                ioff = 0;
+                ibase = 0;
+                if (++ip == rhs) {
+                    ip = 0;
+                    if (++ik < nb) {
+                        di = load_rdesc(my_units_p + ik);
+                        if (ik + 2 < nb && lane == 0) prefetch_l1(my_units_p + ik + 2);
+                        // the next unit's k-pair infos
+                        if (ik + 1 < nb && lane == 0) {
+                            const RowDesc dn = load_rdesc(my_units_p + ik + 1);
+                            if (dn.kind == 0) prefetch_l1(A.kp_info + dn.kp_off + dn.h);
+                        }
+                    }
+                }
+                iinfo = load_info(di, 0);
+            }
+        };
+        __syncwarp();
 #pragma unroll 1
-            for (int s = 0; s < kStages - 1; ++s) issue();
-            int k = 0;
-            while (k < nb) {
-                issue();
-                const unsigned slot_i = computed % kStages;
-                if (!mbar_wait(bar + slot_i, (computed / kStages) & 1)) {
-                    flag_timeout(status);
-                    failed = true;
-                    break;
+        for (int s = 0; s < kStages - 1; ++s) issue();
+        int ck = 0, cp = 0, ci = 0, cbase = 0;  // compute cursor: unit, rhs column, k-pair index
+        RowDesc dc = di;
+        int cinfo = load_info(dc, 0);
+        float D[4][4];
+        long long acc[4];
+        int since = 0;
+#pragma unroll
+        for (int m = 0; m < 4; ++m)
+#pragma unroll
+            for (int r = 0; r < 4; ++r) D[m][r] = 0.f;
+#pragma unroll
+        for (int r = 0; r < 4; ++r) acc[r] = 0;
+        auto fold_row = [&]() {
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                long long v = 0;
+#pragma unroll
+                for (int m = 0; m < 4; ++m) {
+                    v += fold(D[m][r], m);
+                    D[m][r] = 0.f;
                 }
-                const int m = group(k);
-                const uint8_t* slot = slots + slot_i * kSlotBytes;
-                int off = 0;
-                for (int q = 0; q < m; ++q) {
-                    const RowDesc d = desc(k + q);
-                    if (d.block >= 0) {
-                        const uint32_t* SW = reinterpret_cast<const uint32_t*>(slot + off);
-                        const double* ua = W.u + (long long)p * n_comp + d.comp;
-                        const int us = int((reinterpret_cast<uintptr_t>(ua) >> 3) & 1);
-                        const double* SV = reinterpret_cast<const double*>(slot + off + d.words * 4) + us;
-                        off += d.words * 4 + ((d.count + 1) * 8 + 15) / 16 * 16;
-                        // widths from the header, u from the slot
-                        int hw = 0;
-                        double uv = 0.0;
-                        if (lane < d.count) {
-                            hw = int((SW[lane >> 1] >> (16 * (lane & 1))) & 0xFFFFu);
-                            uv = SV[lane];
-                        }
-                        const int eb = __reduce_max_sync(0xFFFFFFFFu, lane < d.count ? exp_field(uv) : 0);
-                        if (eb) {
-                            const long long U = lane < d.count ? to_fixed(uv, eb) : 0;
-                            int4* tab = s_tab[warp];
-                            tab[lane] = make_int4(int(U & kLimbMask), int(U >> kLimb), hw >> 5, (hw & 31) + 1);
-                            __syncwarp();
-                            long long alo0 = 0, ahi0 = 0, alo1 = 0, ahi1 = 0;
-                            long long blo0 = 0, bhi0 = 0, blo1 = 0, bhi1 = 0;
-                            if (r0 < T.rows) {
-                                int j = 0;
-                                for (; j + 1 < d.count; j += 2) {
-                                    const int4 t0 = tab[j], t1 = tab[j + 1];
-                                    int c0, c1, e0, e1;
-                                    row_pair_codes_rt(SW + t0.z, lane, t0.w, c0, c1);
-                                    row_pair_codes_rt(SW + t1.z, lane, t1.w, e0, e1);
-                                    alo0 += (long long)c0 * t0.x;
-                                    ahi0 += (long long)c0 * t0.y;
-                                    alo1 += (long long)c1 * t0.x;
-                                    ahi1 += (long long)c1 * t0.y;
-                                    blo0 += (long long)e0 * t1.x;
-                                    bhi0 += (long long)e0 * t1.y;
-                                    blo1 += (long long)e1 * t1.x;
-                                    bhi1 += (long long)e1 * t1.y;
-                                }
-                                if (j < d.count) {
-                                    const int4 t0 = tab[j];
-                                    int c0, c1;
-                                    row_pair_codes_rt(SW + t0.z, lane, t0.w, c0, c1);
-                                    alo0 += (long long)c0 * t0.x;
-                                    ahi0 += (long long)c0 * t0.y;
-                                    alo1 += (long long)c1 * t0.x;
-                                    ahi1 += (long long)c1 * t0.y;
-                                }
-                            }
-                            alo0 += blo0;
-                            ahi0 += bhi0;
-                            alo1 += blo1;
-                            ahi1 += bhi1;
-                            __syncwarp();
-                            __int128 v0 = widen(ahi0, alo0), v1 = widen(ahi1, alo1);
-                            if (r0 >= T.rows) v0 = 0;
-                            if (r1 >= T.rows) v1 = 0;
-                            add_aligned(acc0, acc1, e_acc, v0, v1, eb);
-                        }
-                    } else {
-                        // column slice of a dense diagonal block (column-major values)
-                        const DenseDesc dd = A.dd[-1 - d.block];
-                        const double* D = A.dense + d.off;
-                        const double* xcp = W.xc + (long long)p * n + dd.col0 + d.words;
-                        double dg0 = 0.0, dg1 = 0.0;
-                        const bool v0 = r0 < T.rows, v1 = r1 < T.rows;
-                        // eight columns at a time: all loads issued before the FMA chain
-                        for (int k0 = 0; k0 < d.count; k0 += 8) {
-                            double xv[8], a0v[8], a1v[8];
+                acc[r] += v;
+            }
+            since = 0;
+        };
+        auto advance = [&]() {
+            if (++cp == rhs) {
+                cp = 0;
+                if (++ck < nb) dc = load_rdesc(my_units_p + ck);
+            }
+            cbase = 0;
+            cinfo = load_info(dc, 0);
+        };
+        while (ck < nb) {
+            if (dc.kind != 0) {
+                // dense slice: rows 2*lane, 2*lane+1 in FP64
+                const RowUnit& U = my_units_p[ck];
+                const int cols = __ldg(&U.cols), ld = __ldg(&U.ld), xcol = __ldg(&U.xcol), rows = __ldg(&U.rows);
+                const double* Dv = A.dense + __ldg(&U.doff);
+                const double* xcp = W.xc + (long long)cp * n + xcol;
+                const int r0 = 2 * lane, r1 = 2 * lane + 1;
+                const bool v0 = r0 < rows, v1 = r1 < rows;
+                double dg0 = 0.0, dg1 = 0.0;
+                for (int k0 = 0; k0 < cols; k0 += 4) {
+                    double xv[4], a0v[4], a1v[4];
 #pragma unroll
-                            for (int q = 0; q < 8; ++q) {
-                                const int kk = k0 + q;
-                                const bool in = kk < d.count;
-                                const double* col = D + (long long)kk * dd.m;
-                                xv[q] = in ? __ldg(xcp + kk) : 0.0;
-                                a0v[q] = (in && v0) ? __ldg(col + r0) : 0.0;
-                                a1v[q] = (in && v1) ? __ldg(col + r1) : 0.0;
-                            }
+                    for (int k = 0; k < 4; ++k) {
+                        const int kk = k0 + k;
+                        const bool in = kk < cols;
+                        const double* col = Dv + (long long)kk * ld;
+                        xv[k] = in ? __ldg(xcp + kk) : 0.0;
+                        a0v[k] = (in && v0) ? __ldg(col + r0) : 0.0;
+                        a1v[k] = (in && v1) ? __ldg(col + r1) : 0.0;
+                    }
 #pragma unroll
-                            for (int q = 0; q < 8; ++q) {
-                                dg0 = fma(a0v[q], xv[q], dg0);
-                                dg1 = fma(a1v[q], xv[q], dg1);
-                            }
-                        }
-                        s_diag[d.comp][r0] = dg0;
-                        s_diag[d.comp][r1] = dg1;
-                        if (lane == 0) atomicMax(&s_nslices, d.comp + 1);
+                    for (int k = 0; k < 4; ++k) {
+                        dg0 = fma(a0v[k], xv[k], dg0);
+                        dg1 = fma(a1v[k], xv[k], dg1);
                     }
                 }
-                k += m;
-                ++computed;
-                __syncwarp();
+                double* pd = W.pdense + ((long long)cp * n_dense_parts + dc.h) * 64;
+                pd[r0] = dg0;
+                pd[r1] = dg1;
+                advance();
+                continue;
             }
-            // after a failed wait the warp does no more work but still takes
-            // part in the tile's barriers below
-        }
-        // row sums go to the warp's own (drained) stage 0 for the combine
-        __int128* wacc = reinterpret_cast<__int128*>(slots);
-        wacc[r0] = acc0;
-        wacc[r1] = acc1;
-        if (lane == 0) s_e[warp] = e_acc;
-        __syncthreads();
-        if (threadIdx.x < T.rows) {
-            const int r = threadIdx.x;
-            int et = 0;
-#pragma unroll
-            for (int i = 0; i < kWarps; ++i) et = max(et, s_e[i]);
-            __int128 tot = 0;
-#pragma unroll
-            for (int i = 0; i < kWarps; ++i) {
-                const int dsh = et - s_e[i];
-                const __int128 a = reinterpret_cast<const __int128*>(smem_raw + (size_t)i * kStages * kSlotBytes)[r];
-                if (dsh == 0) tot += a;
-                else if (dsh < 127) tot += (a + ((__int128)1 << (dsh - 1))) >> dsh;
+            issue();
+            const unsigned slot_i = computed % kStages;
+            if (!mbar_wait(bar + slot_i, (computed / kStages) & 1)) {
+                flag_timeout(status);
+                failed = true;
+                break;
             }
-            const double lr = et ? i128_ldexp(tot, et - 1022 - kFixBits - kGuard) : 0.0;
-            double dg = 0.0;
-            for (int sl = 0; sl < s_nslices; ++sl) dg += s_diag[sl][r];
-            y[(long long)__ldg(A.perm + T.row0 + r) * rhs + p] = dg + lr;
+            const uint8_t* slot = slots + slot_i * kRowSlotBytes;
+            if (ci - cbase == 32) {
+                cbase = ci;
+                cinfo = load_info(dc, cbase);
+            }
+            int cbytes;
+            const int c = row_step_kps(cinfo, dc.nkps, ci, cbase, cbytes);
+            const uint8_t* gp = slot;
+            const uint32_t lrow = smem_u32(slot + cbytes) + 16u * unsigned(lane);
+            for (int k = 0; k < c; ++k) {
+                const int kp = dc.h + (ci + k) * dc.H;
+                const int info = __shfl_sync(0xFFFFFFFFu, cinfo, ci + k - cbase);
+                const int planes = info & 7, nibs = info >> 3;
+                uint32_t b[4];
+                limb_frags(lrow + unsigned(k * 512), b);
+                const int kv = dc.K - 32 * kp;  // k slots of this k-pair inside the k axis
+                if (kv < 32) {
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) {
+                        const int e = 8 * i + 2 * t;
+                        if (e >= kv) b[i] &= 0xFFFF0000u;
+                        if (e + 1 >= kv) b[i] &= 0x0000FFFFu;
+                    }
+                }
+#pragma unroll
+                for (int m = 0; m < 4; ++m)
+                    if (m < planes) {
+                        const bool nib = (nibs >> m) & 1;
+                        group_mma(D[m], gp, nib, 16, g, t, b);
+                        gp += nib ? 256 : 512;
+                    }
+                if (++since == 8) fold_row();
+            }
+            ++computed;
+            ci += c;
+            if (ci == dc.nkps) {
+                fold_row();
+                // row g + 8(t&1): limbs over the row's four lanes
+                __int128 v0 = ((__int128)acc[0] << (16 * t)) + ((__int128)acc[1] << (16 * t + 8));
+                __int128 v1 = ((__int128)acc[2] << (16 * t)) + ((__int128)acc[3] << (16 * t + 8));
+#pragma unroll
+                for (int r = 0; r < 4; ++r) acc[r] = 0;
+                const bool hi = t & 1;
+                __int128 R = hi ? v1 : v0;
+                R += shfl_xor_i128(hi ? v0 : v1, 1);
+                R += shfl_xor_i128(R, 2);
+                const long long tb = ((long long)cp * n_tiles + dc.tile) * 8;
+                if (t < 2) st_i128(W.plr + (tb + dc.q * dc.H + dc.h) * 16 + g + 8 * t, R);
+                ci = 0;
+                advance();
+            }
+            __syncwarp();
         }
-        __syncthreads();
     }
     // copies still in flight (only after a failed wait): wait for them, bounded
     while (computed < issued) {
@@ -817,62 +962,104 @@ __global__ void __launch_bounds__(kWarps * 32, 2) row_kernel(Arena A, Work W, do
     }
 }
 
-// Validation: decode every code through the same device routines the apply
-// kernels use (code_at / row_pair_codes on the resident layout).  Column
-// side: one warp per unit; row side: one warp per tile.
-template <int W>
-__device__ __forceinline__ void col_codes(const uint32_t* cw, int count, int lane, int (&c)[32]) {
-    uint32_t w[W];
+// One warp per (row tile, rhs column): y = dense partials (slice order) +
+// the low-rank row sums minus the tile's offset correction, converted once.
+__global__ void __launch_bounds__(256) combine_kernel(Arena A, Work W, double* __restrict__ y, int n_tiles,
+                                                      int n_kpg, int n_dense_parts, int rhs) {
+    const int lane = threadIdx.x & 31;
+    const long long gw = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (gw >= (long long)n_tiles * rhs) return;
+    const int p = int(gw / n_tiles), tile = int(gw % n_tiles);
+    const RowTile T = A.tiles[tile];
+    const int xe = W.xe[p];
+    __int128 bias = 0;
+    for (int k = lane; k < T.nkpg; k += 32) bias += ld_i128(W.kpbias + (long long)p * n_kpg + T.kpg0 + k);
 #pragma unroll
-    for (int v = 0; v < W; ++v) w[v] = cw[v * count + lane];
-#pragma unroll
-    for (int e = 0; e < 32; ++e) c[e] = code_at<W>(w, e);
+    for (int o = 16; o > 0; o >>= 1) bias += shfl_xor_i128(bias, o);
+    const long long tb = ((long long)p * n_tiles + tile) * 8;
+    for (int r = lane; r < T.rows; r += 32) {
+        __int128 R = -bias;
+        for (int h = 0; h < T.nh; ++h) R += ld_i128(W.plr + (tb + (r >> 4) * T.hsplit + h) * 16 + (r & 15));
+        const double lr = (xe && T.c_exp != kNoExp) ? i128_ldexp(R, xe + T.c_exp - 1022 - kFixBits) : 0.0;
+        double dg = 0.0;
+        for (int sl = 0; sl < T.nslices; ++sl)
+            dg += W.pdense[((long long)p * n_dense_parts + T.dense0 + sl) * 64 + r];
+        y[(long long)__ldg(A.perm + T.row0 + r) * rhs + p] = dg + lr;
+    }
 }
 
-__global__ void decode_col_kernel(Arena A, int n_tasks, const long long* __restrict__ comp_off, int* out) {
-    const int lane = threadIdx.x & 31;
+// Validation: decode every code from the resident layout through the same
+// fragment routines the apply kernels feed to the MMA (group_digits uses the
+// permutes and masks of group_mma).  out[comp_base[c] + i] = code i of
+// component c (i: block column on the right side, clustered row on the left).
+__global__ void decode_col_kernel(Arena A, int n_tasks, const long long* __restrict__ comp_base, int* out) {
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
     const int warps = gridDim.x * (blockDim.x >> 5);
     for (int ti = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); ti < n_tasks; ti += warps) {
         const ColTask T = A.tasks[ti];
-        if (lane >= T.count) continue;
-        const long long o = comp_off[__ldg(A.task_comp + T.comp_idx + lane)];
+        const int P = (T.width + 7) / 8;
+        const bool nibtop = T.width - 8 * (P - 1) <= 4;
+        const int RB = (P - 1) * 32 + (nibtop ? 16 : 32);
         for (int ch = T.chunk0; ch < T.chunk0 + T.nchunks; ++ch) {
-            const uint32_t* cw = A.qwords + T.word0 + (long long)ch * T.stride;
-            int c[32];
-            switch (T.width) {
-#define QH_DEC_CASE(WW) \
-    case WW:            \
-        col_codes<WW>(cw, T.count, lane, c); \
-        break;
-                QH_WIDTH_CASES(QH_DEC_CASE)
-#undef QH_DEC_CASE
-                default:
-                    break;
+            const uint8_t* cb = A.qcodes + T.off + (long long)ch * T.stride;
+            for (int q = 0; q < 2; ++q) {
+                const int rows = min(16, T.count - 16 * q);
+                if (rows <= 0) continue;
+                uint32_t u[2][8] = {};
+                int off = q * 16 * RB;
+                for (int m = 0; m < P; ++m) {
+                    const bool nib = nibtop && m == P - 1;
+                    uint32_t d[2][8];
+                    group_digits(cb + off, nib, rows, g, t, d);
+                    for (int hh = 0; hh < 2; ++hh)
+                        for (int k = 0; k < 8; ++k) u[hh][k] |= d[hh][k] << (8 * m);
+                    off += rows * (nib ? 16 : 32);
+                }
+                for (int hh = 0; hh < 2; ++hh) {
+                    const int j = 16 * q + 8 * hh + g;
+                    if (j >= T.count) continue;
+                    const int c = A.task_rec[T.comp_idx + j].comp;
+                    for (int k = 0; k < 8; ++k) {
+                        const int i = ch * kColChunk + slot_entry(k >> 2, k & 3, t);
+                        if (i < T.n) out[comp_base[c] + i] = int(int64_t(u[hh][k]) - (int64_t(1) << (T.width - 1)));
+                    }
+                }
             }
-            for (int e = 0; e < 32; ++e)
-                if (ch * kColChunk + e < T.n) out[o + ch * kColChunk + e] = c[e];
         }
     }
 }
 
-__global__ void decode_row_kernel(Arena A, int n_tiles, const long long* __restrict__ comp_off, int* out) {
-    const int lane = threadIdx.x & 31;
+__global__ void decode_row_kernel(Arena A, int n_units, const long long* __restrict__ comp_base, int* out) {
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
     const int warps = gridDim.x * (blockDim.x >> 5);
-    for (int t = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); t < n_tiles; t += warps) {
-        const RowTile T = A.tiles[t];
-        for (int it = T.item0; it < T.item1; ++it) {
-            const RowItem I = A.items[it];
-            if (I.block < 0) continue;
-            const uint32_t* blk = A.pwords + I.off;
-            for (int j = 0; j < I.count; ++j) {
-                const int hw = int((blk[j >> 1] >> (16 * (j & 1))) & 0xFFFFu);
-                const int w = (hw & 31) + 1;
-                const uint32_t* piece = blk + (hw >> 5);
-                int c0 = 0, c1 = 0;
-                if (2 * lane < T.rows) row_pair_codes_rt(piece, lane, w, c0, c1);
-                const long long o = comp_off[I.comp + j] + I.rloc0;
-                if (2 * lane < T.rows) out[o + 2 * lane] = c0;
-                if (2 * lane + 1 < T.rows) out[o + 2 * lane + 1] = c1;
+    for (int ui = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); ui < n_units; ui += warps) {
+        const RowUnit U = A.units[ui];
+        if (U.kind != 0) continue;
+        const RowTile T = A.tiles[U.tile];
+        const uint8_t* gp = A.pcodes + U.code_off;
+        for (int i = 0; i < U.nkps; ++i) {
+            const int kp = U.h + i * U.H;
+            const int info = A.kp_info[U.kp_off + kp];
+            const int planes = info & 7, nibs = info >> 3;
+            uint32_t u[2][8] = {};
+            for (int m = 0; m < planes; ++m) {
+                const bool nib = (nibs >> m) & 1;
+                uint32_t d[2][8];
+                group_digits(gp, nib, 16, g, t, d);
+                for (int hh = 0; hh < 2; ++hh)
+                    for (int k = 0; k < 8; ++k) u[hh][k] |= d[hh][k] << (8 * m);
+                gp += nib ? 256 : 512;
+            }
+            for (int hh = 0; hh < 2; ++hh) {
+                const int tr = 16 * U.q + 8 * hh + g;
+                if (tr >= T.rows) continue;
+                for (int k = 0; k < 8; ++k) {
+                    const int e = slot_entry(k >> 2, k & 3, t);
+                    const int c = A.slot_comp[U.slot0 + 32 * i + e];
+                    if (c < 0) continue;
+                    const int w = A.comp_w[c];
+                    out[comp_base[c] + T.row0 + tr] = int(int64_t(u[hh][k]) - (int64_t(1) << (w - 1)));
+                }
             }
         }
     }
@@ -910,6 +1097,10 @@ struct qh_matrix {
     int sms = 1;
     void* arena = nullptr;  // device copy of L.arena
     Arena A{};
+    // unit schedules: warp w of the column (row) grid runs units
+    // warp_off[w] .. warp_off[w + 1] of the (reordered) task (unit) array
+    int* sched = nullptr;
+    int col_grid = 0, row_grid = 0;
     // lazily allocated scratch for calls without a workspace, and host staging
     std::mutex mu;
     void* own_ws = nullptr;
@@ -924,6 +1115,7 @@ struct qh_matrix {
         cudaGetDevice(&prev);
         cudaSetDevice(device);
         if (arena) cudaFree(arena);
+        if (sched) cudaFree(sched);
         if (own_ws) cudaFree(own_ws);
         if (d_status) cudaFree(d_status);
         if (pinned) cudaFreeHost(pinned);
@@ -955,6 +1147,42 @@ int check_device(int device) {
     return QH_OK;
 }
 
+// Longest-first assignment of n units (cost(i)) to W warps: each unit goes to
+// the warp with the least work so far.  Returns the permutation (warp-major,
+// each warp's units heaviest first) and the W + 1 warp offsets.
+template <class F>
+void schedule(int n, int W, F cost, std::vector<int32_t>& order, std::vector<int32_t>& off) {
+    std::vector<int32_t> idx(static_cast<size_t>(n), 0);
+    std::iota(idx.begin(), idx.end(), 0);
+    std::vector<double> c(static_cast<size_t>(n), 0.0);
+    for (int i = 0; i < n; ++i) c[size_t(i)] = cost(i);
+    std::stable_sort(idx.begin(), idx.end(), [&](int32_t a, int32_t b) { return c[size_t(a)] > c[size_t(b)]; });
+    using Load = std::pair<double, int32_t>;
+    std::priority_queue<Load, std::vector<Load>, std::greater<Load>> heap;
+    for (int32_t w = 0; w < W; ++w) heap.push({0.0, w});
+    std::vector<std::vector<int32_t>> lists(static_cast<size_t>(W));
+    for (int32_t i : idx) {
+        Load l = heap.top();
+        heap.pop();
+        lists[size_t(l.second)].push_back(i);
+        l.first += c[size_t(i)];
+        heap.push(l);
+    }
+    order.clear();
+    off.assign(size_t(W) + 1, 0);
+    for (int32_t w = 0; w < W; ++w) {
+        off[size_t(w)] = int32_t(order.size());
+        order.insert(order.end(), lists[size_t(w)].begin(), lists[size_t(w)].end());
+    }
+    off[size_t(W)] = int32_t(order.size());
+}
+
+template <class T>
+void permute(T* a, const std::vector<int32_t>& order) {
+    std::vector<T> tmp(a, a + order.size());
+    for (size_t i = 0; i < order.size(); ++i) a[i] = tmp[size_t(order[i])];
+}
+
 int upload(Layout&& L, int device, qh_matrix** out) {
     int rc = check_device(device);
     if (rc) return rc;
@@ -963,6 +1191,42 @@ int upload(Layout&& L, int device, qh_matrix** out) {
     if (!m) return fail(QH_ERUNTIME, "out of host memory");
     m->L = std::move(L);
     m->device = device;
+    cudaDeviceGetAttribute(&m->sms, cudaDevAttrMultiProcessorCount, device);
+    {
+        // warp schedules for this device's grids (cost ~ bytes moved plus a
+        // fixed cost per unit)
+        Layout& Lm = m->L;
+        m->col_grid = std::max(1, std::min((Lm.n_tasks + kWarps - 1) / kWarps, m->sms * 2));
+        m->row_grid = std::max(1, std::min((Lm.n_units + kWarps - 1) / kWarps, m->sms * 2));
+        auto* tasks = reinterpret_cast<ColTask*>(Lm.arena.data() + Lm.sec.tasks);
+        auto* units = reinterpret_cast<RowUnit*>(Lm.arena.data() + Lm.sec.units);
+        const uint8_t* kpi = Lm.arena.data() + Lm.sec.kp_info;
+        std::vector<int32_t> corder, coff, rorder, roff;
+        schedule(Lm.n_tasks, m->col_grid * kWarps, [&](int i) {
+            const ColTask& T = tasks[i];
+            return double(T.nchunks) * double(T.stride + 512) + 3000.0;
+        }, corder, coff);
+        schedule(Lm.n_units, m->row_grid * kWarps, [&](int i) {
+            const RowUnit& U = units[i];
+            if (U.kind != 0) return 3.0 * U.rows * U.cols * 8 + 2000.0;
+            double b = 0;
+            for (int k = 0; k < U.nkps; ++k) {
+                const int info = kpi[U.kp_off + U.h + int64_t(k) * U.H];
+                b += (info & 7) * 512 - __builtin_popcount(unsigned(info >> 3)) * 256 + 512;
+            }
+            return b + 2000.0;
+        }, rorder, roff);
+        permute(tasks, corder);
+        permute(units, rorder);
+        std::vector<int32_t> sched(coff);
+        sched.insert(sched.end(), roff.begin(), roff.end());
+        cudaError_t e2 = cudaMalloc(&m->sched, 4 * sched.size());
+        if (e2 == cudaSuccess) e2 = cudaMemcpy(m->sched, sched.data(), 4 * sched.size(), cudaMemcpyHostToDevice);
+        if (e2 != cudaSuccess) {
+            delete m;
+            return cuda_fail(e2, "cudaMalloc");
+        }
+    }
     cudaError_t e = cudaMalloc(&m->arena, m->L.sec.total);
     if (e != cudaSuccess) {
         delete m;
@@ -973,10 +1237,9 @@ int upload(Layout&& L, int device, qh_matrix** out) {
         delete m;
         return cuda_fail(e, "cudaMemcpy host-to-device");
     }
-    cudaDeviceGetAttribute(&m->sms, cudaDevAttrMultiProcessorCount, device);
-    e = cudaFuncSetAttribute(row_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kPipeSmem);
+    e = cudaFuncSetAttribute(row_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kRowPipeSmem);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(column_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kPipeSmem);
+        e = cudaFuncSetAttribute(column_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kColPipeSmem);
     if (e != cudaSuccess) {
         delete m;
         return cuda_fail(e, "cudaFuncSetAttribute");
@@ -991,12 +1254,16 @@ int upload(Layout&& L, int device, qh_matrix** out) {
     m->A.comp_w = base + S.comp_w;
     m->A.comp_s = reinterpret_cast<const double*>(base + S.comp_s);
     m->A.tasks = reinterpret_cast<const ColTask*>(base + S.tasks);
-    m->A.task_comp = reinterpret_cast<const int32_t*>(base + S.task_comp);
-    m->A.qwords = reinterpret_cast<const uint32_t*>(base + S.qwords);
-    m->A.pwords = reinterpret_cast<const uint32_t*>(base + S.pwords);
+    m->A.task_rec = reinterpret_cast<const TaskRec*>(base + S.task_rec);
+    m->A.qcodes = base + S.qcodes;
+    m->A.pcodes = base + S.pcodes;
     m->A.dense = reinterpret_cast<const double*>(base + S.dense);
     m->A.tiles = reinterpret_cast<const RowTile*>(base + S.tiles);
-    m->A.items = reinterpret_cast<const RowItem*>(base + S.items);
+    m->A.units = reinterpret_cast<const RowUnit*>(base + S.units);
+    m->A.kp_info = base + S.kp_info;
+    m->A.slot_comp = reinterpret_cast<const int32_t*>(base + S.slot_comp);
+    m->A.kpg_tile = reinterpret_cast<const int32_t*>(base + S.kpg_tile);
+    m->A.comp_part = reinterpret_cast<const int32_t*>(base + S.comp_part);
     *out = m;
     return QH_OK;
 }
@@ -1017,8 +1284,12 @@ int guarded(F&& f) {
 }
 
 struct WsPlan {
-    size_t xc, xl, xe, cnt, part, u, total, zero_bytes;
+    size_t xc, xblk, xe, xq, lsum, lsplit, blimb, kpbias, plr, pdense, total;
+    int nblk;
 };
+
+// x limbs are read by whole 32-entry chunks: pad past the last chunk.
+size_t padded_order(const Layout& L) { return (L.order + kColChunk - 1) / kColChunk * kColChunk + kColChunk; }
 
 WsPlan ws_plan(const Layout& L, size_t rhs) {
     WsPlan w;
@@ -1028,15 +1299,17 @@ WsPlan ws_plan(const Layout& L, size_t rhs) {
         off += align256(std::max<size_t>(bytes, 1));
         return o;
     };
-    // zeroed before each apply: xe and the split counters (contiguous)
+    w.nblk = (L.n_chunks + 7) / 8;
+    w.lsplit = take(8 * 8 * 32 * size_t(L.n_split) * rhs);  // zeroed by prep_x
     w.xe = take(4 * rhs);
-    w.cnt = take(4 * size_t(L.n_split) * rhs);
-    w.zero_bytes = off;
-    // xc and u are read by 16-byte-rounded bulk copies: keep 32 spare bytes
-    w.xc = take(8 * L.order * rhs + 32);
-    w.xl = take(8 * L.order * rhs + 32);
-    w.part = take(16 * 32 * size_t(L.n_split) * size_t(L.max_parts) * rhs);
-    w.u = take(8 * size_t(L.n_comp) * rhs + 32);
+    w.xblk = take(4 * size_t(w.nblk) * rhs);
+    w.xc = take(8 * L.order * rhs);
+    w.xq = take(16 * padded_order(L) * rhs);
+    w.lsum = take(8 * 8 * size_t(L.n_comp) * rhs);
+    w.blimb = take(16 * size_t(L.n_slots) * rhs);
+    w.kpbias = take(16 * size_t(L.n_kpg) * rhs);
+    w.plr = take(16 * 16 * 8 * size_t(L.n_tiles) * rhs);
+    w.pdense = take(8 * 64 * size_t(L.n_dense_parts) * rhs);
     w.total = off;
     return w;
 }
@@ -1051,30 +1324,40 @@ int launch(const qh_matrix* m, const double* x, double* y, size_t rhs, void* ws,
     const WsPlan P = ws_plan(L, rhs);
     Work W;
     W.xc = reinterpret_cast<double*>(w + P.xc);
-    W.xl = reinterpret_cast<int2*>(w + P.xl);
+    W.xblk = reinterpret_cast<int*>(w + P.xblk);
     W.xe = reinterpret_cast<int*>(w + P.xe);
-    W.split_cnt = reinterpret_cast<int*>(w + P.cnt);
-    W.part = reinterpret_cast<long long*>(w + P.part);
-    W.u = reinterpret_cast<double*>(w + P.u);
+    W.xq = reinterpret_cast<uint4*>(w + P.xq);
+    W.lsum = reinterpret_cast<long long*>(w + P.lsum);
+    W.lsplit = reinterpret_cast<long long*>(w + P.lsplit);
+    W.blimb = reinterpret_cast<uint4*>(w + P.blimb);
+    W.kpbias = reinterpret_cast<uint4*>(w + P.kpbias);
+    W.plr = reinterpret_cast<uint4*>(w + P.plr);
+    W.pdense = reinterpret_cast<double*>(w + P.pdense);
     auto mark = [&](int i) {
         if (ev) cudaEventRecord(static_cast<cudaEvent_t>(ev[i]), s);
     };
-    const long long prep_warps = (long long)L.n_chunks * (long long)rhs;
+    const int irhs = int(rhs);
     mark(0);
-    cudaError_t e = cudaMemsetAsync(w, 0, P.zero_bytes, s);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
-    prep_x_kernel<<<unsigned((prep_warps + 7) / 8), 256, 0, s>>>(m->A, W, x, n, int(rhs), L.n_chunks, status);
-    x_limbs_kernel<<<unsigned(((long long)n * (long long)rhs + 255) / 256), 256, 0, s>>>(W, n, int(rhs));
+    prep_x_kernel<<<dim3(unsigned(P.nblk), unsigned(rhs)), 256, 0, s>>>(
+        m->A, W, x, n, irhs, L.n_chunks, reinterpret_cast<int*>(W.lsplit), L.n_split * 32 * 8 * 2 * irhs, status);
+    const int n_pad = int(padded_order(L));
+    x_limbs_kernel<<<dim3(unsigned((n_pad + 255) / 256), unsigned(rhs)), 256, 0, s>>>(W, n, n_pad, P.nblk);
     mark(1);
-    if (L.n_tasks > 0) {
-        const int grid = std::max(1, std::min((L.n_tasks + kWarps - 1) / kWarps, m->sms * 2));
-        column_kernel<<<grid, kWarps * 32, kPipeSmem, s>>>(m->A, W, L.n_tasks, n, int(rhs), L.n_comp, L.max_parts,
-                                                            status);
-    }
+    if (L.n_tasks > 0)
+        column_kernel<<<m->col_grid, kWarps * 32, kColPipeSmem, s>>>(m->A, W, m->sched, n_pad, irhs, L.n_comp,
+                                                                      L.n_split, status);
+    if (L.n_kpg > 0)
+        expand_kernel<<<unsigned(((long long)L.n_kpg * irhs + 7) / 8), 256, 0, s>>>(m->A, W, L.n_kpg, L.n_slots,
+                                                                                    L.n_comp, L.n_split, irhs);
     mark(2);
-    row_kernel<<<L.n_tiles, kWarps * 32, kPipeSmem, s>>>(m->A, W, y, n, int(rhs), L.n_comp, status);
+    if (L.n_units > 0)
+        row_kernel<<<m->row_grid, kWarps * 32, kRowPipeSmem, s>>>(m->A, W, m->sched + m->col_grid * kWarps + 1, n,
+                                                                   irhs, L.n_slots, L.n_tiles, L.n_dense_parts,
+                                                                   status);
+    combine_kernel<<<unsigned(((long long)L.n_tiles * irhs + 7) / 8), 256, 0, s>>>(m->A, W, y, L.n_tiles, L.n_kpg,
+                                                                                  L.n_dense_parts, irhs);
     mark(3);
-    e = cudaGetLastError();
+    cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "CUDA kernel launch");
     return QH_OK;
 }
@@ -1328,13 +1611,18 @@ int qh_debug_decode(const qh_matrix* m, int side, int32_t* out, size_t out_count
             e = cudaMemcpy(lr.data(), m->A.lr, sizeof(LowRankDesc) * lr.size(), cudaMemcpyDeviceToHost);
             if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy device-to-host");
         }
-        // component-major output: component c's codes start at off[c]
+        // component-major output: component c's codes start at off[c]; the
+        // kernels index left codes by clustered row (base off[c] - row0) and
+        // right codes by block column (base off[c])
         std::vector<long long> off(size_t(m->L.n_comp) + 1, 0);
         for (const auto& d : lr)
             for (int j = 0; j < d.rank; ++j)
                 off[size_t(d.comp0 + j) + 1] = side == 0 ? d.m : d.n;
         for (size_t c = 0; c + 1 < off.size(); ++c) off[c + 1] += off[c];
         const size_t total = size_t(off.back());
+        if (side == 0)
+            for (const auto& d : lr)
+                for (int j = 0; j < d.rank; ++j) off[size_t(d.comp0 + j)] -= d.row0;
         if (needed) *needed = total;
         if (!out) return QH_OK;
         if (out_count != total) return fail(QH_EINVAL, "output size does not match the code count");
@@ -1352,7 +1640,7 @@ int qh_debug_decode(const qh_matrix* m, int side, int32_t* out, size_t out_count
             if (side == 1)
                 decode_col_kernel<<<std::max(1, std::min((m->L.n_tasks + 7) / 8, 4096)), 256>>>(m->A, m->L.n_tasks, d_off, d_out);
             else
-                decode_row_kernel<<<std::max(1, std::min((m->L.n_tiles + 7) / 8, 4096)), 256>>>(m->A, m->L.n_tiles, d_off, d_out);
+                decode_row_kernel<<<std::max(1, std::min((m->L.n_units + 7) / 8, 4096)), 256>>>(m->A, m->L.n_units, d_off, d_out);
             e = cudaGetLastError();
         }
         if (e == cudaSuccess) e = cudaMemcpy(out, d_out, sizeof(int) * total, cudaMemcpyDeviceToHost);
