@@ -482,7 +482,7 @@ Layout build_layout(const HostMatrix& m) {
     std::vector<uint8_t> pcodes;
     std::vector<uint8_t> kp_info;
     int64_t n_slots = 0;
-    int32_t n_dense_parts = 0;
+    std::vector<TileDense> tdense;
     std::vector<int32_t> slot_comp;  // component of each B row slot (-1: padding)
     std::vector<int32_t> kpg_tile;   // tile of each B row group
     struct RowComp {
@@ -497,29 +497,15 @@ Layout build_layout(const HostMatrix& m) {
             RowTile T{};
             T.row0 = int32_t(r);
             T.rows = rows;
-            T.dense0 = n_dense_parts;
+            T.dense0 = int32_t(tdense.size());
             std::vector<RowComp> kc;
             for (int32_t k : slab_blocks[s]) {
                 const auto& b = m.blocks[size_t(k)];
                 const int32_t rloc0 = int32_t(r - b.row0);
                 if (b.dense) {
-                    // column slices, one unit each, summed in slice order
                     const DenseDesc& d = dd[size_t(-1 - block_item[size_t(k)])];
-                    const int32_t ns = std::min<int32_t>(kDenseSlices, d.n);
-                    for (int32_t sl = 0; sl < ns; ++sl) {
-                        const int32_t c0 = int32_t(int64_t(d.n) * sl / ns), c1 = int32_t(int64_t(d.n) * (sl + 1) / ns);
-                        RowUnit U{};
-                        U.tile = ti;
-                        U.kind = 1;
-                        U.h = n_dense_parts + T.nslices;
-                        U.cols = c1 - c0;
-                        U.ld = d.m;
-                        U.xcol = d.col0 + c0;
-                        U.rows = rows;
-                        U.doff = d.off + int64_t(c0) * d.m + rloc0;
-                        units.push_back({int64_t(rows) * (c1 - c0) * 8, U});
-                        ++T.nslices;
-                    }
+                    tdense.push_back({d.off + rloc0, d.m, d.n, d.col0, 0});
+                    ++T.ndense;
                     continue;
                 }
                 for (uint64_t j = 0; j < b.rank; ++j)
@@ -576,7 +562,6 @@ Layout build_layout(const HostMatrix& m) {
                 for (int32_t h = 0; h < T.nh; ++h) {
                     RowUnit U{};
                     U.tile = ti;
-                    U.kind = 0;
                     U.q = q;
                     U.h = h;
                     U.H = T.hsplit;
@@ -611,8 +596,7 @@ Layout build_layout(const HostMatrix& m) {
                         }
                     units.push_back({bytes + int64_t(U.nkps) * 512, U});
                 }
-            n_dense_parts += T.nslices;
-            if (T.qrows * T.nh + T.nslices == 0) throw runtime_error("row tile without blocks");
+            if (T.qrows * T.nh + T.ndense == 0) throw runtime_error("row tile without blocks");
             tiles.push_back(T);
         }
     }
@@ -625,7 +609,7 @@ Layout build_layout(const HostMatrix& m) {
     L.n_kpg = int32_t(kpg_tile.size());
     L.n_units = int32_t(unit_list.size());
     L.n_slots = int32_t(n_slots);
-    L.n_dense_parts = n_dense_parts;
+    L.n_tdense = int32_t(tdense.size());
     L.stored_p_bytes = pcodes.size();
     if (qcodes.size() >= (1ull << 42) || pcodes.size() >= (1ull << 42))
         throw overflow_error("packed factors too large for the device layout");
@@ -650,6 +634,7 @@ Layout build_layout(const HostMatrix& m) {
     S.pcodes = place(pcodes.size() + 16);
     S.dense = place(8 * dense_cm.size());
     S.tiles = place(sizeof(RowTile) * tiles.size());
+    S.tdense = place(sizeof(TileDense) * tdense.size());
     S.units = place(sizeof(RowUnit) * unit_list.size());
     S.kp_info = place(kp_info.size() + 16);
     S.slot_comp = place(4 * slot_comp.size());
@@ -679,6 +664,7 @@ Layout build_layout(const HostMatrix& m) {
     if (!comp_part.empty()) std::memcpy(A.data() + S.comp_part, comp_part.data(), 4 * comp_part.size());
     if (!dense_cm.empty()) std::memcpy(A.data() + S.dense, dense_cm.data(), 8 * dense_cm.size());
     if (!tiles.empty()) std::memcpy(A.data() + S.tiles, tiles.data(), sizeof(RowTile) * tiles.size());
+    if (!tdense.empty()) std::memcpy(A.data() + S.tdense, tdense.data(), sizeof(TileDense) * tdense.size());
     return L;
 }
 

@@ -135,30 +135,31 @@ struct DenseDesc {
 };
 // One row tile: clustered rows [row0, row0 + rows) inside one slab; qrows
 // M-tiles, k axis split hsplit ways (nh of the splits have k-pairs); dense
-// slices with partial sums dense0 .. dense0 + nslices - 1; B row groups (32
-// slots each) kpg0 .. kpg0 + nkpg - 1; u is put in fixed point on the
-// exponent field xe + c_exp (xe: the largest exponent field of x).
+// blocks tdense[dense0 .. dense0 + ndense); B row groups (32 slots each)
+// kpg0 .. kpg0 + nkpg - 1; u is put in fixed point on the exponent field
+// xe + c_exp (xe: the largest exponent field of x).
 struct RowTile {
     int32_t row0, rows, qrows, hsplit;
-    int32_t nh, nslices, dense0, c_exp;
+    int32_t nh, ndense, dense0, c_exp;
     int32_t kpg0, nkpg, pad[2];
 };
 static_assert(sizeof(RowTile) == 48, "RowTile layout");
-// One warp's unit of row-side work.  kind 0: rows 16q .. 16q + 15 of a tile
-// over the k-pairs kp = h, h + H, ... (nkps of them; B rows from slot0;
-// digit groups from code_off; the tile's k axis has K slots).  kind 1: a
-// column slice of a dense diagonal block: `cols` columns of stride `ld`
-// starting at element doff (first row = the tile's), x entries from xcol,
-// `rows` rows, dense partial index h.
-struct RowUnit {
-    int32_t tile, kind, q, h;
-    int32_t H, nkps, K, slot0;
-    int64_t code_off, kp_off;
-    int32_t cols, ld, xcol, rows;
-    int64_t doff;
-    int32_t pad[2];
+// A dense diagonal block's part in a row tile: value (tile row r, column k)
+// at dense[off + k * ld + r], x entries from xcol.
+struct TileDense {
+    int64_t off;
+    int32_t ld, cols, xcol, pad;
 };
-static_assert(sizeof(RowUnit) == 80, "RowUnit layout");
+static_assert(sizeof(TileDense) == 24, "TileDense layout");
+// One warp's unit of row-side work: rows 16q .. 16q + 15 of a tile over the
+// k-pairs kp = h, h + H, ... (nkps of them; B rows from slot0; digit groups
+// from code_off; the tile's k axis has K slots).
+struct RowUnit {
+    int32_t tile, q, h, H;
+    int32_t nkps, K, slot0, pad;
+    int64_t code_off, kp_off;
+};
+static_assert(sizeof(RowUnit) == 48, "RowUnit layout");
 
 // Bytes of one column-side shared-memory stage (code groups and x rows of
 // the step's chunks); one row-side stage (code groups and B rows).
@@ -168,8 +169,6 @@ constexpr int kRowSlotBytes = 4096;
 constexpr int kMaxPartChunks = 16;
 // Exponent offset of a row tile without nonzero components.
 constexpr int32_t kNoExp = -4000;
-// Column slices a dense diagonal block is cut into (one per row-side warp).
-constexpr int kDenseSlices = 8;
 
 // Digit planes of a width-w code, and whether its top plane is a nibble.
 inline int code_planes(int w) { return (w + 7) / 8; }
@@ -177,7 +176,7 @@ inline bool top_is_nibble(int w) { return w - 8 * (code_planes(w) - 1) <= 4; }
 
 // Byte offsets of each section inside the device arena.
 struct Sections {
-    size_t perm, lr, dd, comp_w, comp_s, tasks, task_rec, qcodes, pcodes, dense, tiles, units, kp_info,
+    size_t perm, lr, dd, comp_w, comp_s, tasks, task_rec, qcodes, pcodes, dense, tiles, tdense, units, kp_info,
         slot_comp, kpg_tile, comp_part;
     size_t total;
 };
@@ -186,7 +185,7 @@ struct Layout {
     uint64_t order = 0;
     int32_t n_lr = 0, n_dense = 0, n_comp = 0, n_tiles = 0, n_chunks = 0;
     int32_t n_tasks = 0, n_split = 0, max_parts = 1;
-    int32_t n_units = 0, n_slots = 0, n_dense_parts = 0, n_kpg = 0;
+    int32_t n_units = 0, n_slots = 0, n_tdense = 0, n_kpg = 0;
     std::vector<uint8_t> arena;  // host image of the device arena
     Sections sec{};
     double bound = 0;

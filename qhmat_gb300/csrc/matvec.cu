@@ -106,6 +106,7 @@ struct Arena {
     const uint8_t* pcodes;
     const double* dense;
     const RowTile* tiles;
+    const TileDense* tdense;
     const RowUnit* units;
     const uint8_t* kp_info;
     const int32_t* slot_comp;
@@ -118,13 +119,18 @@ struct Work {
     int* xblk;         // [rhs][nblk]         largest exponent field of x per prep block
     int* xe;           // [rhs]               largest exponent field of x
     uint4* xq;         // [rhs][n_pad]        limbs of X (zero past n)
-    long long* lsum;   // [rhs][n_comp][8]    per-limb sums sum_i c_ij limb_l(X_i) of each component
-    long long* lsplit; // [rhs][n_split*32][8] the same for components of split tasks (zeroed by prep)
+    double* u;         // [rhs][n_comp]       u_j = (s^P s^Q) sum_i c_ij x_i (unsplit tasks)
+    long long* lsplit; // [rhs][n_split*32][8] per-limb sums sum_i c_ij limb_l(X_i) of split tasks'
+                       //                     components (zeroed by prep, parts add exactly)
     uint4* blimb;      // [rhs][n_slots]      row-side B rows: limbs of U
     uint4* kpbias;     // [rhs][n_kpg]        sum of 2^(w-1) U over each B row group (128-bit)
     uint4* plr;        // [rhs][n_tiles][8][16] low-rank row sums of each row unit (128-bit)
-    double* pdense;    // [rhs][n_dense_parts][64] dense slice row sums
+    double* pdense;    // [rhs][n_tiles][kDenseSlices][64] dense diagonal row sums per column slice
 };
+
+// Column slices a tile's dense diagonal blocks are cut into (one thread per
+// row and slice in expand_kernel; summed in slice order by combine_kernel).
+constexpr int kDenseSlices = 4;
 
 // -------------------------------------------------- bulk copies (TMA)
 
@@ -577,19 +583,7 @@ __global__ void __launch_bounds__(kWarps * 32, 2) column_kernel(Arena A, Work W,
         for (int s = 0; s < kStages - 1; ++s) issue();
         int ck = 0, cp = 0, cc = 0;  // compute cursor
         ColTask dc = di;
-        // components of this lane's rows (16q + g + 8h), loaded as soon as a
-        // unit starts (used at its end)
-        int rc[2][2];
-        auto load_rows = [&]() {
-#pragma unroll
-            for (int q = 0; q < 2; ++q)
-#pragma unroll
-                for (int hh = 0; hh < 2; ++hh) {
-                    const int row = 16 * q + 8 * hh + g;
-                    rc[q][hh] = row < dc.count ? __ldg(&A.task_rec[dc.comp_idx + row].comp) : -1;
-                }
-        };
-        load_rows();
+        const int xe0 = W.xe[0];
         while (ck < nb) {
             issue();
             const unsigned slot_i = computed % kStages;
@@ -619,35 +613,55 @@ __global__ void __launch_bounds__(kWarps * 32, 2) column_kernel(Arena A, Work W,
                     case 3: col_fold<3>(a); break;
                     default: col_fold<4>(a); break;
                 }
-                // this lane's per-limb sums: rows 16q + g + 8h, limbs 2t, 2t+1
-                // (finished (unit ck, column cp); parts of a split task add
-                // theirs exactly with integer atomics)
+                // this lane's per-limb sums: rows 16q + g + 8h, limbs 2t, 2t+1.
+                // Unsplit task: stage all rows' sums in the consumed slot (not
+                // refilled before the next issue) and let lane j finish row j;
+                // a part of a split task adds its sums exactly with atomics.
+                const int xe = cp == 0 ? xe0 : W.xe[cp];
+                if (dc.nparts == 1) {
+                    long long* st = reinterpret_cast<long long*>(const_cast<uint8_t*>(slot));
+#pragma unroll
+                    for (int q = 0; q < 2; ++q)
+#pragma unroll
+                        for (int hh = 0; hh < 2; ++hh) {
+                            const int row = 16 * q + 8 * hh + g;
+                            *reinterpret_cast<longlong2*>(st + row * 8 + 2 * t) =
+                                make_longlong2(a.acc[q][2 * hh], a.acc[q][2 * hh + 1]);
+                        }
+                    __syncwarp();
+                    if (lane < dc.count) {
+                        const longlong2* r2 = reinterpret_cast<const longlong2*>(st + lane * 8);
+                        __int128 S = 0;
+#pragma unroll
+                        for (int l = 0; l < 4; ++l) {
+                            const longlong2 v = r2[l];
+                            S += ((__int128)v.x << (16 * l)) + ((__int128)v.y << (16 * l + 8));
+                        }
+                        const int4 rec = __ldg(reinterpret_cast<const int4*>(A.task_rec + dc.comp_idx + lane));
+                        W.u[(long long)cp * n_comp + rec.x] =
+                            xe ? i128_ldexp(S, xe - 1022 - kFixBits) * __hiloint2double(rec.w, rec.z) : 0.0;
+                    }
+                } else {
+#pragma unroll
+                    for (int q = 0; q < 2; ++q)
+#pragma unroll
+                        for (int hh = 0; hh < 2; ++hh) {
+                            const int row = 16 * q + 8 * hh + g;
+                            if (row >= dc.count) continue;
+                            unsigned long long* dst = reinterpret_cast<unsigned long long*>(
+                                W.lsplit + ((long long)cp * n_split * 32 + dc.split_id * 32 + row) * 8 + 2 * t);
+                            atomicAdd(dst, (unsigned long long)a.acc[q][2 * hh]);
+                            atomicAdd(dst + 1, (unsigned long long)a.acc[q][2 * hh + 1]);
+                        }
+                }
 #pragma unroll
                 for (int q = 0; q < 2; ++q)
 #pragma unroll
-                    for (int hh = 0; hh < 2; ++hh) {
-                        const long long l0 = a.acc[q][2 * hh], l1 = a.acc[q][2 * hh + 1];
-                        a.acc[q][2 * hh] = a.acc[q][2 * hh + 1] = 0;
-                        const int c = rc[q][hh];
-                        if (c < 0) continue;
-                        if (dc.nparts == 1) {
-                            long long* dst = W.lsum + ((long long)cp * n_comp + c) * 8 + 2 * t;
-                            *reinterpret_cast<longlong2*>(dst) = make_longlong2(l0, l1);
-                        } else {
-                            const int row = 16 * q + 8 * hh + g;
-                            unsigned long long* dst = reinterpret_cast<unsigned long long*>(
-                                W.lsplit + ((long long)cp * n_split * 32 + dc.split_id * 32 + row) * 8 + 2 * t);
-                            atomicAdd(dst, (unsigned long long)l0);
-                            atomicAdd(dst + 1, (unsigned long long)l1);
-                        }
-                    }
+                    for (int r = 0; r < 4; ++r) a.acc[q][r] = 0;
                 cc = 0;
                 if (++cp == rhs) {
                     cp = 0;
-                    if (++ck < nb) {
-                        dc = load_task(my_tasks + ck);
-                        load_rows();
-                    }
+                    if (++ck < nb) dc = load_task(my_tasks + ck);
                 }
             }
             __syncwarp();
@@ -667,12 +681,33 @@ __device__ __forceinline__ int kp_bytes(int info) {
 }
 
 // B rows of the row side: one warp per group of 32 slots (one k-pair of a
-// row unit).  Lane l forms u of the slot's component from its per-limb sums,
-// puts it in fixed point on the tile's exponent and stores its limbs; the
-// group's offset correction sum 2^(w-1) U is reduced over the warp.
-__global__ void __launch_bounds__(256) expand_kernel(Arena A, Work W, int n_kpg, int n_slots, int n_comp,
-                                                     int n_split, int rhs) {
+// row unit).  Lane l takes u of the slot's component (formed here from the
+// per-limb sums for a split task), puts it in fixed point on the tile's
+// exponent and stores its limbs; the group's offset correction
+// sum 2^(w-1) U is reduced over the warp.
+__global__ void __launch_bounds__(256) expand_kernel(Arena A, Work W, int n, int n_kpg, int n_slots, int n_comp,
+                                                     int n_split, int n_tiles, int rhs, int kpg_blocks) {
     const int lane = threadIdx.x & 31;
+    if ((int)blockIdx.x >= kpg_blocks) {
+        // dense diagonal blocks: CTA per (tile, rhs column), thread per
+        // (column slice, row); columns of a slice in order
+        const int b = int(blockIdx.x) - kpg_blocks;
+        const int p = b / n_tiles, tile = b % n_tiles;
+        const int sl = threadIdx.x >> 6, r = threadIdx.x & 63;
+        const RowTile T = A.tiles[tile];
+        double dg = 0.0;
+        if (r < T.rows) {
+            for (int bb = 0; bb < T.ndense; ++bb) {
+                const TileDense D = A.tdense[T.dense0 + bb];
+                const int k0 = D.cols * sl / kDenseSlices, k1 = D.cols * (sl + 1) / kDenseSlices;
+                const double* col = A.dense + D.off + r;
+                const double* xv = W.xc + (long long)p * n + D.xcol;
+                for (int k = k0; k < k1; ++k) dg = fma(__ldg(col + (long long)k * D.ld), __ldg(xv + k), dg);
+            }
+        }
+        W.pdense[(((long long)p * n_tiles + tile) * kDenseSlices + sl) * 64 + r] = dg;
+        return;
+    }
     const long long gw = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (gw >= (long long)n_kpg * rhs) return;
     const int p = int(gw / n_kpg), kpg = int(gw % n_kpg);
@@ -683,14 +718,18 @@ __global__ void __launch_bounds__(256) expand_kernel(Arena A, Work W, int n_kpg,
     long long U = 0;
     int w = 1;
     if (c >= 0) {
-        // t_c = sum_l 2^(8l) (per-limb sums), exactly; u = (s^P s^Q) t 2^(xe - 1022 - kFixBits)
+        double uv;
         const int pr = __ldg(A.comp_part + c);
-        const long long* ls = pr >= 0 ? W.lsplit + ((long long)p * n_split * 32 + pr) * 8
-                                      : W.lsum + ((long long)p * n_comp + c) * 8;
-        __int128 S = 0;
+        if (pr < 0) {
+            uv = W.u[(long long)p * n_comp + c];
+        } else {
+            // split task: t_c = sum_l 2^(8l) (per-limb sums of all parts), exactly
+            const long long* ls = W.lsplit + ((long long)p * n_split * 32 + pr) * 8;
+            __int128 S = 0;
 #pragma unroll
-        for (int l = 0; l < 8; ++l) S += (__int128)__ldcg(ls + l) << (8 * l);
-        const double uv = xe ? i128_ldexp(S, xe - 1022 - kFixBits) * __ldg(A.comp_s + c) : 0.0;
+            for (int l = 0; l < 8; ++l) S += (__int128)__ldcg(ls + l) << (8 * l);
+            uv = xe ? i128_ldexp(S, xe - 1022 - kFixBits) * __ldg(A.comp_s + c) : 0.0;
+        }
         w = __ldg(A.comp_w + c);
         if (uv != 0.0) U = to_fixed(uv, xe + ce);
     }
@@ -701,18 +740,18 @@ __global__ void __launch_bounds__(256) expand_kernel(Arena A, Work W, int n_kpg,
     if (lane == 0) st_i128(W.kpbias + (long long)p * n_kpg + kpg, b);
 }
 
-// The low-rank fields of a row unit's descriptor (cached in L1).
+// A row unit's descriptor (three 16-byte loads, cached in L1).
 struct RowDesc {
     long long code_off, kp_off;
-    int tile, kind, q, h, H, nkps, K, slot0;
+    int tile, q, h, H, nkps, K, slot0;
 };
 
 __device__ __forceinline__ RowDesc load_rdesc(const RowUnit* p) {
     const int4* q = reinterpret_cast<const int4*>(p);
     const int4 a = __ldg(q), b = __ldg(q + 1), c = __ldg(q + 2);
     RowDesc d;
-    d.tile = a.x, d.kind = a.y, d.q = a.z, d.h = a.w;
-    d.H = b.x, d.nkps = b.y, d.K = b.z, d.slot0 = b.w;
+    d.tile = a.x, d.q = a.y, d.h = a.z, d.H = a.w;
+    d.nkps = b.x, d.K = b.y, d.slot0 = b.z;
     d.code_off = (long long)(((unsigned long long)(unsigned)c.y << 32) | (unsigned)c.x);
     d.kp_off = (long long)(((unsigned long long)(unsigned)c.w << 32) | (unsigned)c.z);
     return d;
@@ -742,11 +781,9 @@ __device__ __forceinline__ int row_step_kps(int info_l, int nkps, int i0, int ba
 // the components' U limbs, folding the FP32 sums into 64-bit integers every 8
 // k-pairs (at most 16 k-blocks, below 2^24).  At the end the limbs and planes
 // of each row are combined into an exact 128-bit sum and stored as the unit's
-// partial.  A dense unit (a column slice of a dense diagonal block) computes
-// its rows in FP64.  combine_kernel adds the partials.
+// partial.  combine_kernel adds the partials and the dense diagonal blocks.
 __global__ void __launch_bounds__(kWarps * 32, 2) row_kernel(Arena A, Work W, const int* __restrict__ warp_off,
-                                                             int n, int rhs, int n_slots, int n_tiles,
-                                                             int n_dense_parts, int* status) {
+                                                             int rhs, int n_slots, int n_tiles, int* status) {
     extern __shared__ __align__(16) uint8_t smem_raw[];
     __shared__ __align__(8) uint64_t s_bar[kWarps][kStages];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -772,21 +809,10 @@ __global__ void __launch_bounds__(kWarps * 32, 2) row_kernel(Arena A, Work W, co
         RowDesc di = load_rdesc(my_units_p);
         if (lane < 2 && lane + 1 < nb) prefetch_l1(my_units_p + lane + 1);
         auto load_info = [&](const RowDesc& d, int base) {
-            return (d.kind == 0 && base + lane < d.nkps) ? int(__ldg(A.kp_info + d.kp_off + d.h + (base + lane) * d.H)) : 0;
+            return base + lane < d.nkps ? int(__ldg(A.kp_info + d.kp_off + d.h + (base + lane) * d.H)) : 0;
         };
-        if (di.kind == 0) iinfo = load_info(di, 0);
+        iinfo = load_info(di, 0);
         auto issue = [&]() {
-            while (ik < nb && di.kind != 0) {  // dense units use no slots
-                if (++ip == rhs) {
-                    ip = 0;
-                    if (++ik < nb) {
-                        di = load_rdesc(my_units_p + ik);
-                        if (ik + 2 < nb && lane == 0) prefetch_l1(my_units_p + ik + 2);
-                        ibase = 0;
-                        iinfo = load_info(di, 0);
-                    }
-                }
-            }
             if (ik >= nb) return;
             if (ii - ibase == 32) {
                 ibase = ii;
@@ -818,7 +844,7 @@ __global__ void __launch_bounds__(kWarps * 32, 2) row_kernel(Arena A, Work W, co
                         // the next unit's k-pair infos
                         if (ik + 1 < nb && lane == 0) {
                             const RowDesc dn = load_rdesc(my_units_p + ik + 1);
-                            if (dn.kind == 0) prefetch_l1(A.kp_info + dn.kp_off + dn.h);
+                            prefetch_l1(A.kp_info + dn.kp_off + dn.h);
                         }
                     }
                 }
@@ -862,38 +888,6 @@ __global__ void __launch_bounds__(kWarps * 32, 2) row_kernel(Arena A, Work W, co
             cinfo = load_info(dc, 0);
         };
         while (ck < nb) {
-            if (dc.kind != 0) {
-                // dense slice: rows 2*lane, 2*lane+1 in FP64
-                const RowUnit& U = my_units_p[ck];
-                const int cols = __ldg(&U.cols), ld = __ldg(&U.ld), xcol = __ldg(&U.xcol), rows = __ldg(&U.rows);
-                const double* Dv = A.dense + __ldg(&U.doff);
-                const double* xcp = W.xc + (long long)cp * n + xcol;
-                const int r0 = 2 * lane, r1 = 2 * lane + 1;
-                const bool v0 = r0 < rows, v1 = r1 < rows;
-                double dg0 = 0.0, dg1 = 0.0;
-                for (int k0 = 0; k0 < cols; k0 += 4) {
-                    double xv[4], a0v[4], a1v[4];
-#pragma unroll
-                    for (int k = 0; k < 4; ++k) {
-                        const int kk = k0 + k;
-                        const bool in = kk < cols;
-                        const double* col = Dv + (long long)kk * ld;
-                        xv[k] = in ? __ldg(xcp + kk) : 0.0;
-                        a0v[k] = (in && v0) ? __ldg(col + r0) : 0.0;
-                        a1v[k] = (in && v1) ? __ldg(col + r1) : 0.0;
-                    }
-#pragma unroll
-                    for (int k = 0; k < 4; ++k) {
-                        dg0 = fma(a0v[k], xv[k], dg0);
-                        dg1 = fma(a1v[k], xv[k], dg1);
-                    }
-                }
-                double* pd = W.pdense + ((long long)cp * n_dense_parts + dc.h) * 64;
-                pd[r0] = dg0;
-                pd[r1] = dg1;
-                advance();
-                continue;
-            }
             issue();
             const unsigned slot_i = computed % kStages;
             if (!mbar_wait(bar + slot_i, (computed / kStages) & 1)) {
@@ -962,30 +956,30 @@ __global__ void __launch_bounds__(kWarps * 32, 2) row_kernel(Arena A, Work W, co
     }
 }
 
-// One warp per (row tile, rhs column): y = dense partials (slice order) +
-// the low-rank row sums minus the tile's offset correction, converted once.
-__global__ void __launch_bounds__(256) combine_kernel(Arena A, Work W, double* __restrict__ y, int n_tiles,
-                                                      int n_kpg, int n_dense_parts, int rhs) {
-    const int lane = threadIdx.x & 31;
-    const long long gw = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    if (gw >= (long long)n_tiles * rhs) return;
-    const int p = int(gw / n_tiles), tile = int(gw % n_tiles);
+// One CTA of 64 threads per (row tile, rhs column), one thread per row: y =
+// the dense diagonal row (its column slices' sums in order) + the low-rank
+// row sums minus the tile's offset correction (reduced by each warp from the
+// B row groups), converted once.
+__global__ void __launch_bounds__(64) combine_kernel(Arena A, Work W, double* __restrict__ y, int n, int n_tiles,
+                                                     int n_kpg, int rhs) {
+    const int lane = threadIdx.x & 31, r = threadIdx.x;
+    const int p = blockIdx.y, tile = blockIdx.x;
     const RowTile T = A.tiles[tile];
     const int xe = W.xe[p];
     __int128 bias = 0;
     for (int k = lane; k < T.nkpg; k += 32) bias += ld_i128(W.kpbias + (long long)p * n_kpg + T.kpg0 + k);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) bias += shfl_xor_i128(bias, o);
+    if (r >= T.rows) return;
     const long long tb = ((long long)p * n_tiles + tile) * 8;
-    for (int r = lane; r < T.rows; r += 32) {
-        __int128 R = -bias;
-        for (int h = 0; h < T.nh; ++h) R += ld_i128(W.plr + (tb + (r >> 4) * T.hsplit + h) * 16 + (r & 15));
-        const double lr = (xe && T.c_exp != kNoExp) ? i128_ldexp(R, xe + T.c_exp - 1022 - kFixBits) : 0.0;
-        double dg = 0.0;
-        for (int sl = 0; sl < T.nslices; ++sl)
-            dg += W.pdense[((long long)p * n_dense_parts + T.dense0 + sl) * 64 + r];
-        y[(long long)__ldg(A.perm + T.row0 + r) * rhs + p] = dg + lr;
-    }
+    __int128 R = -bias;
+    for (int h = 0; h < T.nh; ++h) R += ld_i128(W.plr + (tb + (r >> 4) * T.hsplit + h) * 16 + (r & 15));
+    double dg = 0.0;
+    const double* pd = W.pdense + ((long long)p * n_tiles + tile) * kDenseSlices * 64 + r;
+#pragma unroll
+    for (int sl = 0; sl < kDenseSlices; ++sl) dg += __ldcg(pd + sl * 64);
+    const double lr = (xe && T.c_exp != kNoExp) ? i128_ldexp(R, xe + T.c_exp - 1022 - kFixBits) : 0.0;
+    y[(long long)__ldg(A.perm + T.row0 + r) * rhs + p] = dg + lr;
 }
 
 // Validation: decode every code from the resident layout through the same
@@ -1034,7 +1028,6 @@ __global__ void decode_row_kernel(Arena A, int n_units, const long long* __restr
     const int warps = gridDim.x * (blockDim.x >> 5);
     for (int ui = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); ui < n_units; ui += warps) {
         const RowUnit U = A.units[ui];
-        if (U.kind != 0) continue;
         const RowTile T = A.tiles[U.tile];
         const uint8_t* gp = A.pcodes + U.code_off;
         for (int i = 0; i < U.nkps; ++i) {
@@ -1208,7 +1201,6 @@ int upload(Layout&& L, int device, qh_matrix** out) {
         }, corder, coff);
         schedule(Lm.n_units, m->row_grid * kWarps, [&](int i) {
             const RowUnit& U = units[i];
-            if (U.kind != 0) return 3.0 * U.rows * U.cols * 8 + 2000.0;
             double b = 0;
             for (int k = 0; k < U.nkps; ++k) {
                 const int info = kpi[U.kp_off + U.h + int64_t(k) * U.H];
@@ -1260,6 +1252,7 @@ int upload(Layout&& L, int device, qh_matrix** out) {
     m->A.dense = reinterpret_cast<const double*>(base + S.dense);
     m->A.tiles = reinterpret_cast<const RowTile*>(base + S.tiles);
     m->A.units = reinterpret_cast<const RowUnit*>(base + S.units);
+    m->A.tdense = reinterpret_cast<const TileDense*>(base + S.tdense);
     m->A.kp_info = base + S.kp_info;
     m->A.slot_comp = reinterpret_cast<const int32_t*>(base + S.slot_comp);
     m->A.kpg_tile = reinterpret_cast<const int32_t*>(base + S.kpg_tile);
@@ -1284,7 +1277,7 @@ int guarded(F&& f) {
 }
 
 struct WsPlan {
-    size_t xc, xblk, xe, xq, lsum, lsplit, blimb, kpbias, plr, pdense, total;
+    size_t xc, xblk, xe, xq, u, lsplit, blimb, kpbias, plr, pdense, total;
     int nblk;
 };
 
@@ -1305,11 +1298,11 @@ WsPlan ws_plan(const Layout& L, size_t rhs) {
     w.xblk = take(4 * size_t(w.nblk) * rhs);
     w.xc = take(8 * L.order * rhs);
     w.xq = take(16 * padded_order(L) * rhs);
-    w.lsum = take(8 * 8 * size_t(L.n_comp) * rhs);
+    w.u = take(8 * size_t(L.n_comp) * rhs);
     w.blimb = take(16 * size_t(L.n_slots) * rhs);
     w.kpbias = take(16 * size_t(L.n_kpg) * rhs);
     w.plr = take(16 * 16 * 8 * size_t(L.n_tiles) * rhs);
-    w.pdense = take(8 * 64 * size_t(L.n_dense_parts) * rhs);
+    w.pdense = take(8 * 64 * kDenseSlices * size_t(L.n_tiles) * rhs);
     w.total = off;
     return w;
 }
@@ -1327,7 +1320,7 @@ int launch(const qh_matrix* m, const double* x, double* y, size_t rhs, void* ws,
     W.xblk = reinterpret_cast<int*>(w + P.xblk);
     W.xe = reinterpret_cast<int*>(w + P.xe);
     W.xq = reinterpret_cast<uint4*>(w + P.xq);
-    W.lsum = reinterpret_cast<long long*>(w + P.lsum);
+    W.u = reinterpret_cast<double*>(w + P.u);
     W.lsplit = reinterpret_cast<long long*>(w + P.lsplit);
     W.blimb = reinterpret_cast<uint4*>(w + P.blimb);
     W.kpbias = reinterpret_cast<uint4*>(w + P.kpbias);
@@ -1346,16 +1339,16 @@ int launch(const qh_matrix* m, const double* x, double* y, size_t rhs, void* ws,
     if (L.n_tasks > 0)
         column_kernel<<<m->col_grid, kWarps * 32, kColPipeSmem, s>>>(m->A, W, m->sched, n_pad, irhs, L.n_comp,
                                                                       L.n_split, status);
-    if (L.n_kpg > 0)
-        expand_kernel<<<unsigned(((long long)L.n_kpg * irhs + 7) / 8), 256, 0, s>>>(m->A, W, L.n_kpg, L.n_slots,
-                                                                                    L.n_comp, L.n_split, irhs);
+    {
+        const int kpg_blocks = int(((long long)L.n_kpg * irhs + 7) / 8);
+        expand_kernel<<<unsigned(kpg_blocks + L.n_tiles * irhs), 256, 0, s>>>(
+            m->A, W, n, L.n_kpg, L.n_slots, L.n_comp, L.n_split, L.n_tiles, irhs, kpg_blocks);
+    }
     mark(2);
     if (L.n_units > 0)
-        row_kernel<<<m->row_grid, kWarps * 32, kRowPipeSmem, s>>>(m->A, W, m->sched + m->col_grid * kWarps + 1, n,
-                                                                   irhs, L.n_slots, L.n_tiles, L.n_dense_parts,
-                                                                   status);
-    combine_kernel<<<unsigned(((long long)L.n_tiles * irhs + 7) / 8), 256, 0, s>>>(m->A, W, y, L.n_tiles, L.n_kpg,
-                                                                                  L.n_dense_parts, irhs);
+        row_kernel<<<m->row_grid, kWarps * 32, kRowPipeSmem, s>>>(m->A, W, m->sched + m->col_grid * kWarps + 1, irhs,
+                                                                   L.n_slots, L.n_tiles, status);
+    combine_kernel<<<dim3(unsigned(L.n_tiles), unsigned(rhs)), 64, 0, s>>>(m->A, W, y, n, L.n_tiles, L.n_kpg, irhs);
     mark(3);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "CUDA kernel launch");
