@@ -182,6 +182,12 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned b
         : "memory");
 }
 
+// Programmatic dependent launch: a kernel lets its successor start early
+// (launch_dependents) and waits for its predecessor's results (wait) only
+// where it first reads them; without the launch attribute both are no-ops.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 constexpr int kStages = 3;
 constexpr int kWarps = 8;
 constexpr int kColPipeSmem = kWarps * kStages * kColSlotBytes;
@@ -391,6 +397,7 @@ __device__ __forceinline__ __int128 ld_i128(const uint4* p) {
 __global__ void __launch_bounds__(256) prep_x_kernel(Arena A, Work W, const double* __restrict__ x, int n, int rhs,
                                                      int n_chunks, int* zero, int n_zero, int* status) {
     __shared__ int s_m[8];
+    pdl_trigger();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int p = blockIdx.y;
     const int chunk = blockIdx.x * 8 + warp;
@@ -417,6 +424,8 @@ __global__ void __launch_bounds__(256) prep_x_kernel(Arena A, Work W, const doub
 // limbs of X for 256 entries (zero past n).
 __global__ void __launch_bounds__(256) x_limbs_kernel(Work W, int n, int n_pad, int nblk) {
     __shared__ int s_m[8];
+    pdl_trigger();
+    pdl_wait();
     const int p = blockIdx.y, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     int m = 0;
     for (int i = threadIdx.x; i < nblk; i += blockDim.x) m = max(m, W.xblk[(long long)p * nblk + i]);
@@ -534,8 +543,8 @@ __global__ void __launch_bounds__(kWarps * 32, 2) column_kernel(Arena A, Work W,
     const int gw = blockIdx.x * kWarps + warp;
     const int u0 = __ldg(warp_off + gw), my_units = __ldg(warp_off + gw + 1) - u0;
     const ColTask* my_tasks = A.tasks + u0;
+    if (my_units <= 0) pdl_wait();  // (every thread waits before exiting)
     unsigned issued = 0, computed = 0;  // running step counters (slot, phase)
-    bool failed = false;
     ColAcc a;
 #pragma unroll
     for (int q = 0; q < 2; ++q)
@@ -546,10 +555,12 @@ __global__ void __launch_bounds__(kWarps * 32, 2) column_kernel(Arena A, Work W,
 #pragma unroll
     for (int r = 0; r < 4; ++r) a.acc[0][r] = a.acc[1][r] = 0;
     a.since = 0;
+    pdl_trigger();
     if (my_units > 0) {
         const int nb = my_units;
         int ik = 0, ip = 0, ic = 0;  // issue cursor
         ColTask di = load_task(my_tasks);
+        pdl_wait();  // x limbs and exponents of this apply
         auto issue = [&]() {
             if (ik >= nb) return;
             const int nc = min(di.cps, di.nchunks - ic);
@@ -589,7 +600,6 @@ __global__ void __launch_bounds__(kWarps * 32, 2) column_kernel(Arena A, Work W,
             const unsigned slot_i = computed % kStages;
             if (!mbar_wait(bar + slot_i, (computed / kStages) & 1)) {
                 flag_timeout(status);
-                failed = true;
                 break;
             }
             const int nc = min(dc.cps, dc.nchunks - cc);
@@ -687,6 +697,8 @@ __device__ __forceinline__ int kp_bytes(int info) {
 // sum 2^(w-1) U is reduced over the warp.
 __global__ void __launch_bounds__(256) expand_kernel(Arena A, Work W, int n, int n_kpg, int n_slots, int n_comp,
                                                      int n_split, int n_tiles, int rhs, int kpg_blocks) {
+    pdl_trigger();
+    pdl_wait();
     const int lane = threadIdx.x & 31;
     if ((int)blockIdx.x >= kpg_blocks) {
         // dense diagonal blocks: CTA per (tile, rhs column), thread per
@@ -799,7 +811,8 @@ __global__ void __launch_bounds__(kWarps * 32, 2) row_kernel(Arena A, Work W, co
     const int u0 = __ldg(warp_off + gw), my_units = __ldg(warp_off + gw + 1) - u0;
     const RowUnit* my_units_p = A.units + u0;
     unsigned issued = 0, computed = 0;
-    bool failed = false;
+    pdl_trigger();
+    if (my_units <= 0) pdl_wait();
     if (my_units > 0) {
         const int nb = my_units;
         // issue cursor: unit ik, rhs column ip, k-pair index ii (byte offset
@@ -807,6 +820,7 @@ __global__ void __launch_bounds__(kWarps * 32, 2) row_kernel(Arena A, Work W, co
         int ik = 0, ip = 0, ii = 0, ibase = 0, iinfo = 0;
         long long ioff = 0;
         RowDesc di = load_rdesc(my_units_p);
+        pdl_wait();  // B rows of this apply
         if (lane < 2 && lane + 1 < nb) prefetch_l1(my_units_p + lane + 1);
         auto load_info = [&](const RowDesc& d, int base) {
             return base + lane < d.nkps ? int(__ldg(A.kp_info + d.kp_off + d.h + (base + lane) * d.H)) : 0;
@@ -892,7 +906,6 @@ __global__ void __launch_bounds__(kWarps * 32, 2) row_kernel(Arena A, Work W, co
             const unsigned slot_i = computed % kStages;
             if (!mbar_wait(bar + slot_i, (computed / kStages) & 1)) {
                 flag_timeout(status);
-                failed = true;
                 break;
             }
             const uint8_t* slot = slots + slot_i * kRowSlotBytes;
@@ -962,9 +975,11 @@ __global__ void __launch_bounds__(kWarps * 32, 2) row_kernel(Arena A, Work W, co
 // B row groups), converted once.
 __global__ void __launch_bounds__(64) combine_kernel(Arena A, Work W, double* __restrict__ y, int n, int n_tiles,
                                                      int n_kpg, int rhs) {
+    pdl_trigger();
     const int lane = threadIdx.x & 31, r = threadIdx.x;
     const int p = blockIdx.y, tile = blockIdx.x;
     const RowTile T = A.tiles[tile];
+    pdl_wait();
     const int xe = W.xe[p];
     __int128 bias = 0;
     for (int k = lane; k < T.nkpg; k += 32) bias += ld_i128(W.kpbias + (long long)p * n_kpg + T.kpg0 + k);
@@ -1309,6 +1324,23 @@ WsPlan ws_plan(const Layout& L, size_t rhs) {
 
 size_t ws_bytes(const Layout& L, size_t rhs) { return ws_plan(L, rhs).total; }
 
+// Launch with programmatic stream serialization (the kernel may start while
+// its predecessor finishes; it waits in-kernel for the predecessor's results).
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k, static_cast<KArgs>(args)...);
+}
+
 int launch(const qh_matrix* m, const double* x, double* y, size_t rhs, void* ws, cudaStream_t s,
            int* status, void* const* ev = nullptr) {
     const Layout& L = m->L;
@@ -1334,23 +1366,28 @@ int launch(const qh_matrix* m, const double* x, double* y, size_t rhs, void* ws,
     prep_x_kernel<<<dim3(unsigned(P.nblk), unsigned(rhs)), 256, 0, s>>>(
         m->A, W, x, n, irhs, L.n_chunks, reinterpret_cast<int*>(W.lsplit), L.n_split * 32 * 8 * 2 * irhs, status);
     const int n_pad = int(padded_order(L));
-    x_limbs_kernel<<<dim3(unsigned((n_pad + 255) / 256), unsigned(rhs)), 256, 0, s>>>(W, n, n_pad, P.nblk);
+    cudaError_t e = launch_pdl(x_limbs_kernel, dim3(unsigned((n_pad + 255) / 256), unsigned(rhs)), dim3(256), 0, s,
+                               W, n, n_pad, P.nblk);
     mark(1);
-    if (L.n_tasks > 0)
-        column_kernel<<<m->col_grid, kWarps * 32, kColPipeSmem, s>>>(m->A, W, m->sched, n_pad, irhs, L.n_comp,
-                                                                      L.n_split, status);
-    {
+    if (e == cudaSuccess && L.n_tasks > 0)
+        e = launch_pdl(column_kernel, dim3(unsigned(m->col_grid)), dim3(kWarps * 32), size_t(kColPipeSmem), s, m->A,
+                       W, static_cast<const int*>(m->sched), n_pad, irhs, L.n_comp, L.n_split, status);
+    if (e == cudaSuccess) {
         const int kpg_blocks = int(((long long)L.n_kpg * irhs + 7) / 8);
-        expand_kernel<<<unsigned(kpg_blocks + L.n_tiles * irhs), 256, 0, s>>>(
-            m->A, W, n, L.n_kpg, L.n_slots, L.n_comp, L.n_split, L.n_tiles, irhs, kpg_blocks);
+        e = launch_pdl(expand_kernel, dim3(unsigned(kpg_blocks + L.n_tiles * irhs)), dim3(256), 0, s, m->A, W, n,
+                       L.n_kpg, L.n_slots, L.n_comp, L.n_split, L.n_tiles, irhs, kpg_blocks);
     }
     mark(2);
-    if (L.n_units > 0)
-        row_kernel<<<m->row_grid, kWarps * 32, kRowPipeSmem, s>>>(m->A, W, m->sched + m->col_grid * kWarps + 1, irhs,
-                                                                   L.n_slots, L.n_tiles, status);
-    combine_kernel<<<dim3(unsigned(L.n_tiles), unsigned(rhs)), 64, 0, s>>>(m->A, W, y, n, L.n_tiles, L.n_kpg, irhs);
+    if (e == cudaSuccess && L.n_units > 0)
+        e = launch_pdl(row_kernel, dim3(unsigned(m->row_grid)), dim3(kWarps * 32), size_t(kRowPipeSmem), s, m->A, W,
+                       static_cast<const int*>(m->sched + m->col_grid * kWarps + 1), irhs, L.n_slots, L.n_tiles,
+                       status);
+    if (e == cudaSuccess)
+        e = launch_pdl(combine_kernel, dim3(unsigned(L.n_tiles), unsigned(rhs)), dim3(64), 0, s, m->A, W, y, n,
+                       L.n_tiles, L.n_kpg, irhs);
+    if (e != cudaSuccess) return cuda_fail(e, "CUDA kernel launch");
     mark(3);
-    cudaError_t e = cudaGetLastError();
+    e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "CUDA kernel launch");
     return QH_OK;
 }
