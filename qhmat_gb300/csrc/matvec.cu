@@ -2,37 +2,32 @@
 //
 // y = A x for a matrix held as dense FP64 diagonal blocks plus low-rank blocks
 // whose balanced factors P (rows) and Q (columns) are stored as per-component
-// signed integer codes of width w_j in [2, 32], bit-packed LSB-first exactly
-// as the reference packs them (src/qhmat/core.cpp:235-267), with one FP64
-// scale per factor and component.  The words are permuted for coalesced
-// access (layout.hpp); each code keeps its reference bits.
+// signed integer codes of width w_j in [2, 32] (src/qhmat/core.cpp:235-282),
+// with one FP64 scale per factor and component.  The resident layout
+// (layout.hpp) keeps each code's bits, re-ordered into tensor-core fragment
+// order as base-256 digit planes.
 //
-// FP64 throughput on GB300 is a small fraction of its integer throughput, so
-// the per-code arithmetic is exact integer arithmetic and FP64 is used only
-// per component, per output row and for the dense diagonal blocks:
+// FP64 throughput on GB300 is a small fraction of its tensor throughput, so
+// every code product is an exact small-integer product on the f16 tensor
+// cores (digits <= 255 times 8-bit limbs of a fixed-point operand, FP32 sums
+// that stay integers below 2^24), and FP64 is used only per component, per
+// output row and for the dense diagonal blocks:
 //
-//   prep_x    x (source order) -> clustered order, fixed point: each chunk of
-//             32 clustered entries gets one exponent e and entries
-//             X = round(x * 2^(54-e)), |X| <= 2^54 (plus an FP64 clustered
-//             copy for the dense diagonal blocks).
-//   column    one warp per task of <= 32 components sharing a column range
-//   side      and a width, one component per lane: t = sum_k cQ_k X_k exactly
-//             (codes times the two 27-bit limbs of X, int64 accumulation
-//             folded into a two-word integer every 32 entries), then
-//             u = (s^P s^Q) * t in FP64, one conversion per component.
-//   row side  one CTA per tile of <= 64 rows of one elementary row slab, its
-//             eight warps splitting the blocks covering the tile; two rows per
-//             lane.  A block's u are put in fixed point on the block's own
-//             exponent (U, two 27-bit limbs), sum_j cP_ij U_j is exact, and
-//             the block sum is shifted onto the tile's exponent (16 guard
-//             bits) into a 128-bit accumulator; dense diagonal rows in FP64;
-//             warps combine in shared memory in a fixed order; one writer per
-//             y entry (deterministic, no atomics).
+//   prep_x / x_limbs   x (source order) -> clustered order; one exponent per
+//                      rhs column; X = round(x 2^(62-e)) as eight f16 limbs.
+//   column_kernel      warp per task (<= 32 components sharing a column range
+//                      and a width): t_j = sum_i c_ij X_i exactly, then
+//                      u_j = (s^P s^Q) t_j 2^(e-1022-62) in FP64.
+//   expand_kernel      u of each row tile's components in fixed point on the
+//                      tile's exponent (a layout-time bound), as limb rows;
+//                      plus the dense diagonal blocks in FP64.
+//   row_kernel         warp per (row tile, 16 rows, k split): sum_j c_ij U_j
+//                      exactly, stored as 128-bit partial sums.
+//   combine_kernel     thread per row: partials -> y (one conversion).
 //
-// The only rounding steps are the fixed-point conversions of x (2^-55 relative
-// to the block's largest |x|) and u (2^-55 relative to the block's largest
-// |u|), the product s^P s^Q, the alignment of blocks more than 2^16 below the
-// tile's largest, and the final FP64 conversions: the result agrees with the
+// The only rounding steps are the fixed-point conversions of x and u (2^-63
+// of the column's largest |x|, of the tile's bound on |u|), the product
+// s^P s^Q, and the final FP64 conversions: the result agrees with the
 // reference's FP64 matmul (src/qhmat/core.cpp:360-390) to ~1e-15 in norm.
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
@@ -188,10 +183,22 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned b
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
-constexpr int kStages = 3;
+// Pipeline depth and CTAs per SM of the two streaming kernels (measured:
+// two stages per warp and two CTAs of 8 warps per SM; capping registers for a
+// third CTA spills the accumulators).
+#ifndef QH_COL_STAGES
+#define QH_COL_STAGES 2
+#define QH_COL_CTAS 2
+#endif
+#ifndef QH_ROW_STAGES
+#define QH_ROW_STAGES 2
+#define QH_ROW_CTAS 2
+#endif
+constexpr int kColStages = QH_COL_STAGES;
+constexpr int kRowStages = QH_ROW_STAGES;
 constexpr int kWarps = 8;
-constexpr int kColPipeSmem = kWarps * kStages * kColSlotBytes;
-constexpr int kRowPipeSmem = kWarps * kStages * kRowSlotBytes;
+constexpr int kColPipeSmem = kWarps * kColStages * kColSlotBytes;
+constexpr int kRowPipeSmem = kWarps * kRowStages * kRowSlotBytes;
 
 // Status bits written by the kernels (status word of the apply).
 constexpr int kStatusNonfinite = 1;
@@ -516,9 +523,9 @@ __device__ __forceinline__ void col_step(ColAcc& a, const uint8_t* slot, int nc,
 
 // Column side.  Warp gw owns the units warp_off[gw] .. warp_off[gw + 1]
 // (assigned longest first at upload, heaviest first per warp); its work
-// is the sequence (unit, rhs column, chunk), streamed through a kStages-deep
+// is the sequence (unit, rhs column, chunk), streamed through a kColStages-deep
 // pipeline of shared-memory slots filled by bulk copies (the chunks' code
-// groups and the limbs of their x entries), kStages - 1 steps ahead of their
+// groups and the limbs of their x entries), kColStages - 1 steps ahead of their
 // use.  Per chunk the warp runs, for each M-tile and digit plane, two
 // 16x8x16 MMAs (digits x the eight x limbs), plus two with an all-ones A for
 // sum_i X_i (the offset-code correction); the FP32 sums are folded into 64-bit
@@ -526,17 +533,17 @@ __device__ __forceinline__ void col_step(ColAcc& a, const uint8_t* slot, int nc,
 // limbs and planes are combined into exact 128-bit sums t_j = sum_i c_ij X_i,
 // and lane (g, t) converts component 16(t>>1) + 8(t&1) + g to
 // u_j = (s^P s^Q) t_j 2^(xe - 1022 - kFixBits).
-__global__ void __launch_bounds__(kWarps * 32, 2) column_kernel(Arena A, Work W, const int* __restrict__ warp_off,
+__global__ void __launch_bounds__(kWarps * 32, QH_COL_CTAS) column_kernel(Arena A, Work W, const int* __restrict__ warp_off,
                                                                 int n_pad, int rhs, int n_comp, int n_split,
                                                                 int* status) {
     extern __shared__ __align__(16) uint8_t smem_raw[];
-    __shared__ __align__(8) uint64_t s_bar[kWarps][kStages];
+    __shared__ __align__(8) uint64_t s_bar[kWarps][kColStages];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int g = lane >> 2, t = lane & 3;
-    uint8_t* slots = smem_raw + (size_t)warp * kStages * kColSlotBytes;
+    uint8_t* slots = smem_raw + (size_t)warp * kColStages * kColSlotBytes;
     uint64_t* bar = s_bar[warp];
     if (lane == 0) {
-        for (int i = 0; i < kStages; ++i) mbar_init(bar + i, 1);
+        for (int i = 0; i < kColStages; ++i) mbar_init(bar + i, 1);
         mbar_init_fence();
     }
     __syncwarp();
@@ -564,7 +571,7 @@ __global__ void __launch_bounds__(kWarps * 32, 2) column_kernel(Arena A, Work W,
         auto issue = [&]() {
             if (ik >= nb) return;
             const int nc = min(di.cps, di.nchunks - ic);
-            const unsigned slot_i = issued % kStages;
+            const unsigned slot_i = issued % kColStages;
             uint8_t* slot = slots + slot_i * kColSlotBytes;
             const unsigned wbytes = unsigned(nc * di.stride);
             const unsigned xbytes = unsigned(nc * kColChunk * 16);
@@ -591,14 +598,14 @@ __global__ void __launch_bounds__(kWarps * 32, 2) column_kernel(Arena A, Work W,
         if (lane < 2 && lane + 1 < nb) prefetch_l1(my_tasks + lane + 1);
         __syncwarp();
 #pragma unroll 1
-        for (int s = 0; s < kStages - 1; ++s) issue();
+        for (int s = 0; s < kColStages - 1; ++s) issue();
         int ck = 0, cp = 0, cc = 0;  // compute cursor
         ColTask dc = di;
         const int xe0 = W.xe[0];
         while (ck < nb) {
             issue();
-            const unsigned slot_i = computed % kStages;
-            if (!mbar_wait(bar + slot_i, (computed / kStages) & 1)) {
+            const unsigned slot_i = computed % kColStages;
+            if (!mbar_wait(bar + slot_i, (computed / kColStages) & 1)) {
                 flag_timeout(status);
                 break;
             }
@@ -679,7 +686,7 @@ __global__ void __launch_bounds__(kWarps * 32, 2) column_kernel(Arena A, Work W,
     }
     // copies still in flight (only after a failed wait): wait for them, bounded
     while (computed < issued) {
-        mbar_wait(bar + computed % kStages, (computed / kStages) & 1);
+        mbar_wait(bar + computed % kColStages, (computed / kColStages) & 1);
         ++computed;
     }
 }
@@ -788,22 +795,22 @@ __device__ __forceinline__ int row_step_kps(int info_l, int nkps, int i0, int ba
 // Row side.  Warp gw owns the units warp_off[gw] .. warp_off[gw + 1]
 // (assigned longest first at upload).  A
 // low-rank unit (rows 16q.. of a tile, k-pairs h, h + H, ...) streams its
-// digit groups and B rows through a kStages-deep bulk-copy pipeline; per
+// digit groups and B rows through a kRowStages-deep bulk-copy pipeline; per
 // k-pair it runs, for each plane, two 16x8x16 MMAs of its 16 rows of digits by
 // the components' U limbs, folding the FP32 sums into 64-bit integers every 8
 // k-pairs (at most 16 k-blocks, below 2^24).  At the end the limbs and planes
 // of each row are combined into an exact 128-bit sum and stored as the unit's
 // partial.  combine_kernel adds the partials and the dense diagonal blocks.
-__global__ void __launch_bounds__(kWarps * 32, 2) row_kernel(Arena A, Work W, const int* __restrict__ warp_off,
+__global__ void __launch_bounds__(kWarps * 32, QH_ROW_CTAS) row_kernel(Arena A, Work W, const int* __restrict__ warp_off,
                                                              int rhs, int n_slots, int n_tiles, int* status) {
     extern __shared__ __align__(16) uint8_t smem_raw[];
-    __shared__ __align__(8) uint64_t s_bar[kWarps][kStages];
+    __shared__ __align__(8) uint64_t s_bar[kWarps][kRowStages];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int g = lane >> 2, t = lane & 3;
-    uint8_t* slots = smem_raw + (size_t)warp * kStages * kRowSlotBytes;
+    uint8_t* slots = smem_raw + (size_t)warp * kRowStages * kRowSlotBytes;
     uint64_t* bar = s_bar[warp];
     if (lane == 0) {
-        for (int i = 0; i < kStages; ++i) mbar_init(bar + i, 1);
+        for (int i = 0; i < kRowStages; ++i) mbar_init(bar + i, 1);
         mbar_init_fence();
     }
     __syncwarp();
@@ -834,7 +841,7 @@ __global__ void __launch_bounds__(kWarps * 32, 2) row_kernel(Arena A, Work W, co
             }
             int cbytes;
             const int c = row_step_kps(iinfo, di.nkps, ii, ibase, cbytes);
-            const unsigned slot_i = issued % kStages;
+            const unsigned slot_i = issued % kRowStages;
             uint8_t* slot = slots + slot_i * kRowSlotBytes;
             const unsigned lbytes = unsigned(c * 512);
             if (lane == 0) {
@@ -867,7 +874,7 @@ __global__ void __launch_bounds__(kWarps * 32, 2) row_kernel(Arena A, Work W, co
         };
         __syncwarp();
 #pragma unroll 1
-        for (int s = 0; s < kStages - 1; ++s) issue();
+        for (int s = 0; s < kRowStages - 1; ++s) issue();
         int ck = 0, cp = 0, ci = 0, cbase = 0;  // compute cursor: unit, rhs column, k-pair index
         RowDesc dc = di;
         int cinfo = load_info(dc, 0);
@@ -903,8 +910,8 @@ __global__ void __launch_bounds__(kWarps * 32, 2) row_kernel(Arena A, Work W, co
         };
         while (ck < nb) {
             issue();
-            const unsigned slot_i = computed % kStages;
-            if (!mbar_wait(bar + slot_i, (computed / kStages) & 1)) {
+            const unsigned slot_i = computed % kRowStages;
+            if (!mbar_wait(bar + slot_i, (computed / kRowStages) & 1)) {
                 flag_timeout(status);
                 break;
             }
@@ -964,7 +971,7 @@ __global__ void __launch_bounds__(kWarps * 32, 2) row_kernel(Arena A, Work W, co
     }
     // copies still in flight (only after a failed wait): wait for them, bounded
     while (computed < issued) {
-        mbar_wait(bar + computed % kStages, (computed / kStages) & 1);
+        mbar_wait(bar + computed % kRowStages, (computed / kRowStages) & 1);
         ++computed;
     }
 }
