@@ -165,6 +165,24 @@ def dist_setup():
     return world, rank, local
 
 
+def max_over_ranks(value: float, pg=None, device=None) -> float:
+    """The largest of every rank's value (the whole job ends with its slowest
+    replica); the value itself on one rank."""
+    if pg is None:
+        return float(value)
+    import torch
+
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_gbs(model_bytes: int, world: int, ms_per_step: float) -> float:
+    """Whole-job throughput of `world` replicas, each moving `model_bytes` per
+    step, over the slowest replica's time per step."""
+    return model_bytes * world / (ms_per_step * 1e-3) / 1e9
+
+
 def run_reference_arm(args):
     world, rank, _ = dist_setup()
     if rank != 0:
@@ -316,11 +334,7 @@ def main():
         wall = time.perf_counter() - wall0
         if pg:
             pg.barrier()
-    total_ms = t_start.elapsed_time(t_end)
-    if pg:
-        t = torch.tensor([total_ms], device=dev)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(t_start.elapsed_time(t_end), pg, dev)
     ms_step = total_ms / K
     # per-kernel durations over the timed steps
     kern = {"prep_x": [], "column": [], "row": []}
@@ -362,7 +376,7 @@ def main():
             traffic = json.loads(traffic_file.read_text()).get(dom)
         except ValueError:
             traffic = None
-    value = model * world / (ms_step * 1e-3) / 1e9
+    value = whole_job_gbs(model, world, ms_step)
 
     # parity of the timed result against the oracle (same inputs)
     y_gpu = yd.cpu().numpy()
