@@ -431,7 +431,7 @@ Layout build_layout(const HostMatrix& m) {
             const int32_t nparts = (nchunks + kMaxPartChunks - 1) / kMaxPartChunks;
             const int32_t split_id = nparts > 1 ? n_split++ : -1;
             if (split_id >= 0)
-                for (int32_t l = 0; l < count; ++l) comp_part[size_t(comps[t0 + l].second)] = split_id * 32 + l;
+                for (int32_t l = 0; l < count; ++l) comp_part[size_t(comps[t0 + l].second)] = split_id * 33 + l;
             L.max_parts = std::max(L.max_parts, nparts);
             const int32_t cps = std::max<int32_t>(1, kColSlotBytes / (stride + kColChunk * 16));
             for (int32_t pt = 0; pt < nparts; ++pt) {
@@ -483,8 +483,8 @@ Layout build_layout(const HostMatrix& m) {
     std::vector<uint8_t> kp_info;
     int64_t n_slots = 0;
     std::vector<TileDense> tdense;
-    std::vector<int32_t> slot_comp;  // component of each B row slot (-1: padding)
-    std::vector<int32_t> kpg_tile;   // tile of each B row group
+    std::vector<SlotRec> slot_rec;   // each B row slot's component, split row and width
+    std::vector<int32_t> kpg_cexp;   // exponent offset of each B row group's tile
     struct RowComp {
         int w;
         int32_t comp;
@@ -550,9 +550,14 @@ Layout build_layout(const HostMatrix& m) {
                 for (int32_t kp = h; kp < Kp; kp += T.hsplit) {
                     for (int e = 0; e < 32; ++e) {
                         const int32_t k = 32 * kp + e;
-                        slot_comp.push_back(k < K ? kc[size_t(k)].comp : -1);
+                        if (k < K) {
+                            const int32_t c = kc[size_t(k)].comp;
+                            slot_rec.push_back({c, ((comp_part[size_t(c)] + 1) << 8) | int32_t(m.width[size_t(c)])});
+                        } else {
+                            slot_rec.push_back({-1, 1});
+                        }
                     }
-                    kpg_tile.push_back(ti);
+                    kpg_cexp.push_back(T.c_exp);
                 }
                 n_slots += 32 * int64_t((Kp - h + T.hsplit - 1) / T.hsplit);
             }
@@ -606,7 +611,7 @@ Layout build_layout(const HostMatrix& m) {
     std::vector<RowUnit> unit_list;
     for (const auto& u : units) unit_list.push_back(u.second);
     L.n_tiles = int32_t(tiles.size());
-    L.n_kpg = int32_t(kpg_tile.size());
+    L.n_kpg = int32_t(kpg_cexp.size());
     L.n_units = int32_t(unit_list.size());
     L.n_slots = int32_t(n_slots);
     L.n_tdense = int32_t(tdense.size());
@@ -637,9 +642,8 @@ Layout build_layout(const HostMatrix& m) {
     S.tdense = place(sizeof(TileDense) * tdense.size());
     S.units = place(sizeof(RowUnit) * unit_list.size());
     S.kp_info = place(kp_info.size() + 16);
-    S.slot_comp = place(4 * slot_comp.size());
-    S.kpg_tile = place(4 * kpg_tile.size());
-    S.comp_part = place(4 * comp_part.size());
+    S.slot_rec = place(sizeof(SlotRec) * slot_rec.size());
+    S.kpg_cexp = place(4 * kpg_cexp.size());
     S.total = off;
 
     L.arena.assign(S.total, 0);
@@ -659,9 +663,8 @@ Layout build_layout(const HostMatrix& m) {
     if (!pcodes.empty()) std::memcpy(A.data() + S.pcodes, pcodes.data(), pcodes.size());
     if (!kp_info.empty()) std::memcpy(A.data() + S.kp_info, kp_info.data(), kp_info.size());
     if (!unit_list.empty()) std::memcpy(A.data() + S.units, unit_list.data(), sizeof(RowUnit) * unit_list.size());
-    if (!slot_comp.empty()) std::memcpy(A.data() + S.slot_comp, slot_comp.data(), 4 * slot_comp.size());
-    if (!kpg_tile.empty()) std::memcpy(A.data() + S.kpg_tile, kpg_tile.data(), 4 * kpg_tile.size());
-    if (!comp_part.empty()) std::memcpy(A.data() + S.comp_part, comp_part.data(), 4 * comp_part.size());
+    if (!slot_rec.empty()) std::memcpy(A.data() + S.slot_rec, slot_rec.data(), sizeof(SlotRec) * slot_rec.size());
+    if (!kpg_cexp.empty()) std::memcpy(A.data() + S.kpg_cexp, kpg_cexp.data(), 4 * kpg_cexp.size());
     if (!dense_cm.empty()) std::memcpy(A.data() + S.dense, dense_cm.data(), 8 * dense_cm.size());
     if (!tiles.empty()) std::memcpy(A.data() + S.tiles, tiles.data(), sizeof(RowTile) * tiles.size());
     if (!tdense.empty()) std::memcpy(A.data() + S.tdense, tdense.data(), sizeof(TileDense) * tdense.size());

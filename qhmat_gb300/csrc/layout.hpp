@@ -161,6 +161,13 @@ struct RowUnit {
 };
 static_assert(sizeof(RowUnit) == 48, "RowUnit layout");
 
+// A row-side B row slot: its component (-1: padding past the tile's k axis)
+// and (split row + 1) << 8 | width (split row: the component's row in the
+// partial sums of a split column task, as split_id * 33 + row; 0: unsplit).
+struct SlotRec {
+    int32_t comp, info;
+};
+
 // Bytes of one column-side shared-memory stage (code groups and x rows of
 // the step's chunks); one row-side stage (code groups and B rows).
 constexpr int kColSlotBytes = 4608;
@@ -177,7 +184,7 @@ inline bool top_is_nibble(int w) { return w - 8 * (code_planes(w) - 1) <= 4; }
 // Byte offsets of each section inside the device arena.
 struct Sections {
     size_t perm, lr, dd, comp_w, comp_s, tasks, task_rec, qcodes, pcodes, dense, tiles, tdense, units, kp_info,
-        slot_comp, kpg_tile, comp_part;
+        slot_rec, kpg_cexp;
     size_t total;
 };
 

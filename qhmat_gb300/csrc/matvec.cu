@@ -78,15 +78,29 @@ __device__ __forceinline__ long long to_fixed(double v, int emax) {
     return bits < 0 ? -q : q;
 }
 
-// The eight limbs of X as f16 values (limb k in half k): X = sum_k l_k 2^(8k).
+__device__ __forceinline__ uint32_t prmt(uint32_t a, uint32_t b, uint32_t sel) {
+    uint32_t r;
+    asm("prmt.b32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(sel));
+    return r;
+}
+__device__ __forceinline__ uint32_t hsub2(uint32_t a, uint32_t b) {
+    uint32_t r;
+    asm("sub.f16x2 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b));
+    return r;
+}
+
+// The eight limbs of X (|X| <= 2^62) as f16 values, limb k in half k:
+// X = sum_{k<7} l_k 2^(8k) + l_7 2^56 with l_0..l_6 in [0, 255] and l_7 in
+// [-64, 64].  The bytes of X + 2^62 are those limbs, the top one plus 64;
+// byte b becomes the f16 1024 + b (exponent bits 0x64 above it) and then the
+// integer b by one exact subtraction per pair.
 __device__ __forceinline__ uint4 to_limbs(long long X) {
-    uint32_t h[8];
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-        const int v = k < 7 ? int((X >> (8 * k)) & 255) : int(X >> 56);
-        h[k] = __half_as_ushort(__int2half_rn(v));
-    }
-    return make_uint4(h[0] | (h[1] << 16), h[2] | (h[3] << 16), h[4] | (h[5] << 16), h[6] | (h[7] << 16));
+    const unsigned long long Y = (unsigned long long)X + (1ull << 62);
+    const uint32_t lo = uint32_t(Y), hi = uint32_t(Y >> 32);
+    return make_uint4(hsub2(prmt(lo, 0x64646464u, 0x4140u), 0x64006400u),
+                      hsub2(prmt(lo, 0x64646464u, 0x4342u), 0x64006400u),
+                      hsub2(prmt(hi, 0x64646464u, 0x4140u), 0x64006400u),
+                      hsub2(prmt(hi, 0x64646464u, 0x4342u), 0x64406400u));
 }
 
 struct Arena {
@@ -104,9 +118,8 @@ struct Arena {
     const TileDense* tdense;
     const RowUnit* units;
     const uint8_t* kp_info;
-    const int32_t* slot_comp;
-    const int32_t* kpg_tile;
-    const int32_t* comp_part;
+    const SlotRec* slot_rec;
+    const int32_t* kpg_cexp;
 };
 
 struct Work {
@@ -115,8 +128,8 @@ struct Work {
     int* xe;           // [rhs]               largest exponent field of x
     uint4* xq;         // [rhs][n_pad]        limbs of X (zero past n)
     double* u;         // [rhs][n_comp]       u_j = (s^P s^Q) sum_i c_ij x_i (unsplit tasks)
-    long long* lsplit; // [rhs][n_split*32][8] per-limb sums sum_i c_ij limb_l(X_i) of split tasks'
-                       //                     components (zeroed by prep, parts add exactly)
+    long long* lsplit; // [rhs][n_split*33][8] per-limb sums sum_i c_ij limb_l(X_i) of split tasks'
+                       //                     components (rows split_id*33 + j; zeroed by prep)
     uint4* blimb;      // [rhs][n_slots]      row-side B rows: limbs of U
     uint4* kpbias;     // [rhs][n_kpg]        sum of 2^(w-1) U over each B row group (128-bit)
     uint4* plr;        // [rhs][n_tiles][8][16] low-rank row sums of each row unit (128-bit)
@@ -125,7 +138,7 @@ struct Work {
 
 // Column slices a tile's dense diagonal blocks are cut into (one thread per
 // row and slice in expand_kernel; summed in slice order by combine_kernel).
-constexpr int kDenseSlices = 4;
+constexpr int kDenseSlices = 8;
 
 // -------------------------------------------------- bulk copies (TMA)
 
@@ -256,11 +269,6 @@ __device__ __forceinline__ __int128 shfl_xor_i128(__int128 v, int m) {
 // exact and every accumulator value is an integer times 2^-24 below 1, exact
 // in FP32.
 
-__device__ __forceinline__ uint32_t prmt(uint32_t a, uint32_t b, uint32_t sel) {
-    uint32_t r;
-    asm("prmt.b32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(sel));
-    return r;
-}
 // Byte group word (digits of entries 2t, 2t+1, 2t+8, 2t+9): the f16 pairs of
 // entries (2t, 2t+1) and (2t+8, 2t+9).
 __device__ __forceinline__ uint32_t dig_lo(uint32_t w) { return prmt(w, 0u, 0x4140u); }
@@ -310,11 +318,6 @@ __device__ __forceinline__ void group_mma(float (&d)[4], const uint8_t* grp, boo
 // The top plane of a column task: stored digits s = d + 2^(t-1) become the
 // signed digit d as a normal f16 (1024 + s, minus hb = 1024 + 2^(t-1) in both
 // halves), so no offset correction is needed on the column side.
-__device__ __forceinline__ uint32_t hsub2(uint32_t a, uint32_t b) {
-    uint32_t r;
-    asm("sub.f16x2 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b));
-    return r;
-}
 __device__ __forceinline__ uint32_t top_lo(uint32_t w, uint32_t hb) { return hsub2(prmt(w, 0x64646464u, 0x4140u), hb); }
 __device__ __forceinline__ uint32_t top_hi(uint32_t w, uint32_t hb) { return hsub2(prmt(w, 0x64646464u, 0x4342u), hb); }
 __device__ __forceinline__ uint32_t top_nib(uint32_t v, int k, uint32_t hb) {
@@ -666,7 +669,7 @@ __global__ void __launch_bounds__(kWarps * 32, QH_COL_CTAS) column_kernel(Arena 
                             const int row = 16 * q + 8 * hh + g;
                             if (row >= dc.count) continue;
                             unsigned long long* dst = reinterpret_cast<unsigned long long*>(
-                                W.lsplit + ((long long)cp * n_split * 32 + dc.split_id * 32 + row) * 8 + 2 * t);
+                                W.lsplit + ((long long)cp * n_split * 33 + dc.split_id * 33 + row) * 8 + 2 * t);
                             atomicAdd(dst, (unsigned long long)a.acc[q][2 * hh]);
                             atomicAdd(dst + 1, (unsigned long long)a.acc[q][2 * hh + 1]);
                         }
@@ -710,9 +713,9 @@ __global__ void __launch_bounds__(256) expand_kernel(Arena A, Work W, int n, int
     if ((int)blockIdx.x >= kpg_blocks) {
         // dense diagonal blocks: CTA per (tile, rhs column), thread per
         // (column slice, row); columns of a slice in order
-        const int b = int(blockIdx.x) - kpg_blocks;
-        const int p = b / n_tiles, tile = b % n_tiles;
-        const int sl = threadIdx.x >> 6, r = threadIdx.x & 63;
+        const int b = int(blockIdx.x) - kpg_blocks;  // two CTAs per (tile, rhs column)
+        const int p = (b >> 1) / n_tiles, tile = (b >> 1) % n_tiles;
+        const int sl = (b & 1) * 4 + (threadIdx.x >> 6), r = threadIdx.x & 63;
         const RowTile T = A.tiles[tile];
         double dg = 0.0;
         if (r < T.rows) {
@@ -731,29 +734,27 @@ __global__ void __launch_bounds__(256) expand_kernel(Arena A, Work W, int n, int
     if (gw >= (long long)n_kpg * rhs) return;
     const int p = int(gw / n_kpg), kpg = int(gw % n_kpg);
     const int slot = kpg * 32 + lane;
-    const int c = __ldg(A.slot_comp + slot);
-    const int ce = __ldg(&A.tiles[__ldg(A.kpg_tile + kpg)].c_exp);
+    const int2 rec = __ldg(reinterpret_cast<const int2*>(A.slot_rec + slot));
+    const int ce = __ldg(A.kpg_cexp + kpg);
     const int xe = W.xe[p];
+    const int c = rec.x, w = rec.y & 255, pr = (rec.y >> 8) - 1;
     long long U = 0;
-    int w = 1;
     if (c >= 0) {
         double uv;
-        const int pr = __ldg(A.comp_part + c);
         if (pr < 0) {
             uv = W.u[(long long)p * n_comp + c];
         } else {
             // split task: t_c = sum_l 2^(8l) (per-limb sums of all parts), exactly
-            const long long* ls = W.lsplit + ((long long)p * n_split * 32 + pr) * 8;
+            const long long* ls = W.lsplit + ((long long)p * n_split * 33 + pr) * 8;
             __int128 S = 0;
 #pragma unroll
             for (int l = 0; l < 8; ++l) S += (__int128)__ldcg(ls + l) << (8 * l);
             uv = xe ? i128_ldexp(S, xe - 1022 - kFixBits) * __ldg(A.comp_s + c) : 0.0;
         }
-        w = __ldg(A.comp_w + c);
         if (uv != 0.0) U = to_fixed(uv, xe + ce);
     }
     W.blimb[(long long)p * n_slots + slot] = to_limbs(U);
-    __int128 b = (__int128)U << (w - 1);
+    __int128 b = (__int128)U << (c >= 0 ? w - 1 : 0);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) b += shfl_xor_i128(b, o);
     if (lane == 0) st_i128(W.kpbias + (long long)p * n_kpg + kpg, b);
@@ -986,22 +987,26 @@ __global__ void __launch_bounds__(64) combine_kernel(Arena A, Work W, double* __
     const int lane = threadIdx.x & 31, r = threadIdx.x;
     const int p = blockIdx.y, tile = blockIdx.x;
     const RowTile T = A.tiles[tile];
+    const int rr = r < T.rows ? r : 0;
+    const int out = __ldg(A.perm + T.row0 + rr);
     pdl_wait();
     const int xe = W.xe[p];
+    // every load depends only on the tile: issue them together
+    const long long tb = ((long long)p * n_tiles + tile) * 8;
+    __int128 R = 0;
+    for (int h = 0; h < T.nh; ++h) R += ld_i128(W.plr + (tb + (rr >> 4) * T.hsplit + h) * 16 + (rr & 15));
+    double dg = 0.0;
+    const double* pd = W.pdense + ((long long)p * n_tiles + tile) * kDenseSlices * 64 + rr;
+#pragma unroll
+    for (int sl = 0; sl < kDenseSlices; ++sl) dg += __ldcg(pd + sl * 64);
     __int128 bias = 0;
     for (int k = lane; k < T.nkpg; k += 32) bias += ld_i128(W.kpbias + (long long)p * n_kpg + T.kpg0 + k);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) bias += shfl_xor_i128(bias, o);
     if (r >= T.rows) return;
-    const long long tb = ((long long)p * n_tiles + tile) * 8;
-    __int128 R = -bias;
-    for (int h = 0; h < T.nh; ++h) R += ld_i128(W.plr + (tb + (r >> 4) * T.hsplit + h) * 16 + (r & 15));
-    double dg = 0.0;
-    const double* pd = W.pdense + ((long long)p * n_tiles + tile) * kDenseSlices * 64 + r;
-#pragma unroll
-    for (int sl = 0; sl < kDenseSlices; ++sl) dg += __ldcg(pd + sl * 64);
+    R -= bias;
     const double lr = (xe && T.c_exp != kNoExp) ? i128_ldexp(R, xe + T.c_exp - 1022 - kFixBits) : 0.0;
-    y[(long long)__ldg(A.perm + T.row0 + r) * rhs + p] = dg + lr;
+    y[(long long)out * rhs + p] = dg + lr;
 }
 
 // Validation: decode every code from the resident layout through the same
@@ -1070,7 +1075,7 @@ __global__ void decode_row_kernel(Arena A, int n_units, const long long* __restr
                 if (tr >= T.rows) continue;
                 for (int k = 0; k < 8; ++k) {
                     const int e = slot_entry(k >> 2, k & 3, t);
-                    const int c = A.slot_comp[U.slot0 + 32 * i + e];
+                    const int c = A.slot_rec[U.slot0 + 32 * i + e].comp;
                     if (c < 0) continue;
                     const int w = A.comp_w[c];
                     out[comp_base[c] + T.row0 + tr] = int(int64_t(u[hh][k]) - (int64_t(1) << (w - 1)));
@@ -1276,9 +1281,8 @@ int upload(Layout&& L, int device, qh_matrix** out) {
     m->A.units = reinterpret_cast<const RowUnit*>(base + S.units);
     m->A.tdense = reinterpret_cast<const TileDense*>(base + S.tdense);
     m->A.kp_info = base + S.kp_info;
-    m->A.slot_comp = reinterpret_cast<const int32_t*>(base + S.slot_comp);
-    m->A.kpg_tile = reinterpret_cast<const int32_t*>(base + S.kpg_tile);
-    m->A.comp_part = reinterpret_cast<const int32_t*>(base + S.comp_part);
+    m->A.slot_rec = reinterpret_cast<const SlotRec*>(base + S.slot_rec);
+    m->A.kpg_cexp = reinterpret_cast<const int32_t*>(base + S.kpg_cexp);
     *out = m;
     return QH_OK;
 }
@@ -1315,7 +1319,7 @@ WsPlan ws_plan(const Layout& L, size_t rhs) {
         return o;
     };
     w.nblk = (L.n_chunks + 7) / 8;
-    w.lsplit = take(8 * 8 * 32 * size_t(L.n_split) * rhs);  // zeroed by prep_x
+    w.lsplit = take(8 * 8 * 33 * size_t(L.n_split) * rhs);  // zeroed by prep_x
     w.xe = take(4 * rhs);
     w.xblk = take(4 * size_t(w.nblk) * rhs);
     w.xc = take(8 * L.order * rhs);
@@ -1371,7 +1375,7 @@ int launch(const qh_matrix* m, const double* x, double* y, size_t rhs, void* ws,
     const int irhs = int(rhs);
     mark(0);
     prep_x_kernel<<<dim3(unsigned(P.nblk), unsigned(rhs)), 256, 0, s>>>(
-        m->A, W, x, n, irhs, L.n_chunks, reinterpret_cast<int*>(W.lsplit), L.n_split * 32 * 8 * 2 * irhs, status);
+        m->A, W, x, n, irhs, L.n_chunks, reinterpret_cast<int*>(W.lsplit), L.n_split * 33 * 8 * 2 * irhs, status);
     const int n_pad = int(padded_order(L));
     cudaError_t e = launch_pdl(x_limbs_kernel, dim3(unsigned((n_pad + 255) / 256), unsigned(rhs)), dim3(256), 0, s,
                                W, n, n_pad, P.nblk);
@@ -1381,7 +1385,7 @@ int launch(const qh_matrix* m, const double* x, double* y, size_t rhs, void* ws,
                        W, static_cast<const int*>(m->sched), n_pad, irhs, L.n_comp, L.n_split, status);
     if (e == cudaSuccess) {
         const int kpg_blocks = int(((long long)L.n_kpg * irhs + 7) / 8);
-        e = launch_pdl(expand_kernel, dim3(unsigned(kpg_blocks + L.n_tiles * irhs)), dim3(256), 0, s, m->A, W, n,
+        e = launch_pdl(expand_kernel, dim3(unsigned(kpg_blocks + 2 * L.n_tiles * irhs)), dim3(256), 0, s, m->A, W, n,
                        L.n_kpg, L.n_slots, L.n_comp, L.n_split, L.n_tiles, irhs, kpg_blocks);
     }
     mark(2);
