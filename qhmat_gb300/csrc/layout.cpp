@@ -485,6 +485,7 @@ Layout build_layout(const HostMatrix& m) {
     std::vector<TileDense> tdense;
     std::vector<SlotRec> slot_rec;   // each B row slot's component, split row and width
     std::vector<int32_t> kpg_cexp;   // exponent offset of each B row group's tile
+    std::vector<uint32_t> row_steps; // pipeline steps of the row units
     struct RowComp {
         int w;
         int32_t comp;
@@ -576,6 +577,25 @@ Layout build_layout(const HostMatrix& m) {
                     U.code_off = int64_t(pcodes.size());
                     U.kp_off = kp_off;
                     int64_t bytes = 0;
+                    // pipeline steps: consecutive k-pairs (digit groups and
+                    // 512 bytes of B rows each) filling a row-side stage
+                    U.step0 = int32_t(row_steps.size());
+                    {
+                        int sc = 0, sb = 0;
+                        for (int32_t kp = h; kp < Kp; kp += T.hsplit) {
+                            int cb = 0;
+                            for (int mm = 0; mm < kplanes[size_t(kp)]; ++mm) cb += ((knib[size_t(kp)] >> mm) & 1) ? 256 : 512;
+                            if (sc && sb + cb + 512 * (sc + 1) > kRowSlotBytes) {
+                                row_steps.push_back(uint32_t(sc) | uint32_t(sb / 256) << 8);
+                                sc = 0;
+                                sb = 0;
+                            }
+                            ++sc;
+                            sb += cb;
+                        }
+                        if (sc) row_steps.push_back(uint32_t(sc) | uint32_t(sb / 256) << 8);
+                    }
+                    U.nsteps = int32_t(row_steps.size()) - U.step0;
                     for (int32_t kp = h; kp < Kp; kp += T.hsplit)
                         for (int mm = 0; mm < kplanes[size_t(kp)]; ++mm) {
                             const bool nb = (knib[size_t(kp)] >> mm) & 1;
@@ -644,6 +664,7 @@ Layout build_layout(const HostMatrix& m) {
     S.kp_info = place(kp_info.size() + 16);
     S.slot_rec = place(sizeof(SlotRec) * slot_rec.size());
     S.kpg_cexp = place(4 * kpg_cexp.size());
+    S.row_steps = place(4 * row_steps.size());
     S.total = off;
 
     L.arena.assign(S.total, 0);
@@ -665,6 +686,7 @@ Layout build_layout(const HostMatrix& m) {
     if (!unit_list.empty()) std::memcpy(A.data() + S.units, unit_list.data(), sizeof(RowUnit) * unit_list.size());
     if (!slot_rec.empty()) std::memcpy(A.data() + S.slot_rec, slot_rec.data(), sizeof(SlotRec) * slot_rec.size());
     if (!kpg_cexp.empty()) std::memcpy(A.data() + S.kpg_cexp, kpg_cexp.data(), 4 * kpg_cexp.size());
+    if (!row_steps.empty()) std::memcpy(A.data() + S.row_steps, row_steps.data(), 4 * row_steps.size());
     if (!dense_cm.empty()) std::memcpy(A.data() + S.dense, dense_cm.data(), 8 * dense_cm.size());
     if (!tiles.empty()) std::memcpy(A.data() + S.tiles, tiles.data(), sizeof(RowTile) * tiles.size());
     if (!tdense.empty()) std::memcpy(A.data() + S.tdense, tdense.data(), sizeof(TileDense) * tdense.size());

@@ -153,13 +153,15 @@ struct TileDense {
 static_assert(sizeof(TileDense) == 24, "TileDense layout");
 // One warp's unit of row-side work: rows 16q .. 16q + 15 of a tile over the
 // k-pairs kp = h, h + H, ... (nkps of them; B rows from slot0; digit groups
-// from code_off; the tile's k axis has K slots).
+// from code_off; the tile's k axis has K slots), streamed in nsteps pipeline
+// steps described by row_steps[step0 ..] (k-pairs | code bytes / 256 << 8).
 struct RowUnit {
     int32_t tile, q, h, H;
-    int32_t nkps, K, slot0, pad;
+    int32_t nkps, K, slot0, nsteps;
     int64_t code_off, kp_off;
+    int32_t step0, pad[3];
 };
-static_assert(sizeof(RowUnit) == 48, "RowUnit layout");
+static_assert(sizeof(RowUnit) == 64, "RowUnit layout");
 
 // A row-side B row slot: its component (-1: padding past the tile's k axis)
 // and (split row + 1) << 8 | width (split row: the component's row in the
@@ -184,7 +186,7 @@ inline bool top_is_nibble(int w) { return w - 8 * (code_planes(w) - 1) <= 4; }
 // Byte offsets of each section inside the device arena.
 struct Sections {
     size_t perm, lr, dd, comp_w, comp_s, tasks, task_rec, qcodes, pcodes, dense, tiles, tdense, units, kp_info,
-        slot_rec, kpg_cexp;
+        slot_rec, kpg_cexp, row_steps;
     size_t total;
 };
 

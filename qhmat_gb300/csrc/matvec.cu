@@ -120,6 +120,7 @@ struct Arena {
     const uint8_t* kp_info;
     const SlotRec* slot_rec;
     const int32_t* kpg_cexp;
+    const uint32_t* row_steps;
 };
 
 struct Work {
@@ -760,37 +761,34 @@ __global__ void __launch_bounds__(256) expand_kernel(Arena A, Work W, int n, int
     if (lane == 0) st_i128(W.kpbias + (long long)p * n_kpg + kpg, b);
 }
 
-// A row unit's descriptor (three 16-byte loads, cached in L1).
+// A row unit's descriptor (four 16-byte loads, cached in L1).
 struct RowDesc {
     long long code_off, kp_off;
-    int tile, q, h, H, nkps, K, slot0;
+    int tile, q, h, H, nkps, K, slot0, nsteps, step0;
 };
 
 __device__ __forceinline__ RowDesc load_rdesc(const RowUnit* p) {
     const int4* q = reinterpret_cast<const int4*>(p);
-    const int4 a = __ldg(q), b = __ldg(q + 1), c = __ldg(q + 2);
+    const int4 a = __ldg(q), b = __ldg(q + 1), c = __ldg(q + 2), e = __ldg(q + 3);
     RowDesc d;
     d.tile = a.x, d.q = a.y, d.h = a.z, d.H = a.w;
-    d.nkps = b.x, d.K = b.y, d.slot0 = b.z;
+    d.nkps = b.x, d.K = b.y, d.slot0 = b.z, d.nsteps = b.w;
     d.code_off = (long long)(((unsigned long long)(unsigned)c.y << 32) | (unsigned)c.x);
     d.kp_off = (long long)(((unsigned long long)(unsigned)c.w << 32) | (unsigned)c.z);
+    d.step0 = e.x;
     return d;
 }
 
-// k-pairs [i0, i0 + c) of a row unit that one step carries (digit groups and
-// limb rows), at least one; info_l = this lane's k-pair info (k-pair
-// i0 + lane of the unit's sequence, as loaded for the unit's first 32).
-__device__ __forceinline__ int row_step_kps(int info_l, int nkps, int i0, int base, int& code_bytes) {
-    int bytes = 0, c = 0;
-    code_bytes = 0;
-    while (i0 + c < nkps && c < 32 - (i0 - base)) {
-        const int cb = kp_bytes(__shfl_sync(0xFFFFFFFFu, info_l, i0 - base + c));
-        if (c && bytes + cb + 512 > kRowSlotBytes) break;
-        bytes += cb + 512;
-        code_bytes += cb;
-        ++c;
+// The digit groups of one k-pair with P planes (nibble top plane if NIBTOP),
+// at compile-time offsets.
+template <int P, bool NIBTOP>
+__device__ __forceinline__ void kp_groups(float (&D)[4][4], const uint8_t* gp, int g, int t, const uint32_t (&b)[4]) {
+#pragma unroll
+    for (int m = 0; m < P; ++m) {
+        const bool nib = NIBTOP && m == P - 1;
+        group_mma(D[m], gp, nib, 16, g, t, b);
+        gp += nib ? 256 : 512;
     }
-    return c;
 }
 
 // Row side.  Warp gw owns the units warp_off[gw] .. warp_off[gw + 1]
@@ -823,25 +821,29 @@ __global__ void __launch_bounds__(kWarps * 32, QH_ROW_CTAS) row_kernel(Arena A, 
     if (my_units <= 0) pdl_wait();
     if (my_units > 0) {
         const int nb = my_units;
-        // issue cursor: unit ik, rhs column ip, k-pair index ii (byte offset
-        // ioff); k-pair infos of the unit's k-pairs ibase .. ibase + 31, one per lane
-        int ik = 0, ip = 0, ii = 0, ibase = 0, iinfo = 0;
+        // issue cursor: unit ik, rhs column ip, step is (k-pair index ii,
+        // byte offset ioff); the unit's step words isb .. isb + 31, one per lane
+        int ik = 0, ip = 0, is = 0, isb = 0, ii = 0;
         long long ioff = 0;
         RowDesc di = load_rdesc(my_units_p);
         pdl_wait();  // B rows of this apply
         if (lane < 2 && lane + 1 < nb) prefetch_l1(my_units_p + lane + 1);
+        auto load_steps = [&](const RowDesc& d, int base) {
+            return base + lane < d.nsteps ? __ldg(A.row_steps + d.step0 + base + lane) : 0u;
+        };
         auto load_info = [&](const RowDesc& d, int base) {
             return base + lane < d.nkps ? int(__ldg(A.kp_info + d.kp_off + d.h + (base + lane) * d.H)) : 0;
         };
-        iinfo = load_info(di, 0);
+        uint32_t isteps = load_steps(di, 0);
         auto issue = [&]() {
             if (ik >= nb) return;
-            if (ii - ibase == 32) {
-                ibase = ii;
-                iinfo = load_info(di, ibase);
+            if (is - isb == 32) {
+                isb = is;
+                isteps = load_steps(di, isb);
             }
-            int cbytes;
-            const int c = row_step_kps(iinfo, di.nkps, ii, ibase, cbytes);
+            const uint32_t sw = __shfl_sync(0xFFFFFFFFu, isteps, is - isb);
+            const int c = int(sw & 255u);
+            const int cbytes = int(sw >> 8) * 256;
             const unsigned slot_i = issued % kRowStages;
             uint8_t* slot = slots + slot_i * kRowSlotBytes;
             const unsigned lbytes = unsigned(c * 512);
@@ -852,32 +854,36 @@ __global__ void __launch_bounds__(kWarps * 32, QH_ROW_CTAS) row_kernel(Arena A, 
                 bulk_load(slot + cbytes, W.blimb + (long long)ip * n_slots + di.slot0 + 32 * ii, lbytes, bar + slot_i);
             }
             ++issued;
+            ++is;
             ii += c;
             ioff += cbytes;
-            if (ii == di.nkps) {
-                ii = 0;
+            if (is == di.nsteps) {
+                is = isb = ii = 0;
                 ioff = 0;
-                ibase = 0;
                 if (++ip == rhs) {
                     ip = 0;
                     if (++ik < nb) {
                         di = load_rdesc(my_units_p + ik);
                         if (ik + 2 < nb && lane == 0) prefetch_l1(my_units_p + ik + 2);
-                        // the next unit's k-pair infos
+                        // the next unit's step words and k-pair infos
                         if (ik + 1 < nb && lane == 0) {
                             const RowDesc dn = load_rdesc(my_units_p + ik + 1);
+                            prefetch_l1(A.row_steps + dn.step0);
                             prefetch_l1(A.kp_info + dn.kp_off + dn.h);
                         }
                     }
                 }
-                iinfo = load_info(di, 0);
+                isteps = load_steps(di, 0);
             }
         };
         __syncwarp();
 #pragma unroll 1
         for (int s = 0; s < kRowStages - 1; ++s) issue();
-        int ck = 0, cp = 0, ci = 0, cbase = 0;  // compute cursor: unit, rhs column, k-pair index
+        // compute cursor: unit ck, rhs column cp, step cs (words csb ..), k-pair
+        // index ci (infos cib ..)
+        int ck = 0, cp = 0, cs = 0, csb = 0, ci = 0, cib = 0;
         RowDesc dc = di;
+        uint32_t csteps = load_steps(dc, 0);
         int cinfo = load_info(dc, 0);
         float D[4][4];
         long long acc[4];
@@ -906,7 +912,8 @@ __global__ void __launch_bounds__(kWarps * 32, QH_ROW_CTAS) row_kernel(Arena A, 
                 cp = 0;
                 if (++ck < nb) dc = load_rdesc(my_units_p + ck);
             }
-            cbase = 0;
+            cs = csb = ci = cib = 0;
+            csteps = load_steps(dc, 0);
             cinfo = load_info(dc, 0);
         };
         while (ck < nb) {
@@ -917,18 +924,22 @@ __global__ void __launch_bounds__(kWarps * 32, QH_ROW_CTAS) row_kernel(Arena A, 
                 break;
             }
             const uint8_t* slot = slots + slot_i * kRowSlotBytes;
-            if (ci - cbase == 32) {
-                cbase = ci;
-                cinfo = load_info(dc, cbase);
+            if (cs - csb == 32) {
+                csb = cs;
+                csteps = load_steps(dc, csb);
             }
-            int cbytes;
-            const int c = row_step_kps(cinfo, dc.nkps, ci, cbase, cbytes);
+            const uint32_t sw = __shfl_sync(0xFFFFFFFFu, csteps, cs - csb);
+            const int c = int(sw & 255u);
+            const int cbytes = int(sw >> 8) * 256;
             const uint8_t* gp = slot;
             const uint32_t lrow = smem_u32(slot + cbytes) + 16u * unsigned(lane);
             for (int k = 0; k < c; ++k) {
+                if (ci + k - cib == 32) {
+                    cib = ci + k;
+                    cinfo = load_info(dc, cib);
+                }
                 const int kp = dc.h + (ci + k) * dc.H;
-                const int info = __shfl_sync(0xFFFFFFFFu, cinfo, ci + k - cbase);
-                const int planes = info & 7, nibs = info >> 3;
+                const int info = __shfl_sync(0xFFFFFFFFu, cinfo, ci + k - cib);
                 uint32_t b[4];
                 limb_frags(lrow + unsigned(k * 512), b);
                 const int kv = dc.K - 32 * kp;  // k slots of this k-pair inside the k axis
@@ -940,18 +951,31 @@ __global__ void __launch_bounds__(kWarps * 32, QH_ROW_CTAS) row_kernel(Arena A, 
                         if (e + 1 >= kv) b[i] &= 0x0000FFFFu;
                     }
                 }
+                switch (info) {  // planes | nibble planes << 3: the widths 32, 24, 16, 12, 8, 4
+                    case 4: kp_groups<4, false>(D, gp, g, t, b); break;
+                    case 3: kp_groups<3, false>(D, gp, g, t, b); break;
+                    case 2: kp_groups<2, false>(D, gp, g, t, b); break;
+                    case 2 | (2 << 3): kp_groups<2, true>(D, gp, g, t, b); break;
+                    case 1: kp_groups<1, false>(D, gp, g, t, b); break;
+                    case 1 | (1 << 3): kp_groups<1, true>(D, gp, g, t, b); break;
+                    default: {
+                        const int planes = info & 7, nibs = info >> 3;
+                        const uint8_t* q = gp;
 #pragma unroll
-                for (int m = 0; m < 4; ++m)
-                    if (m < planes) {
-                        const bool nib = (nibs >> m) & 1;
-                        group_mma(D[m], gp, nib, 16, g, t, b);
-                        gp += nib ? 256 : 512;
+                        for (int m = 0; m < 4; ++m)
+                            if (m < planes) {
+                                const bool nib = (nibs >> m) & 1;
+                                group_mma(D[m], q, nib, 16, g, t, b);
+                                q += nib ? 256 : 512;
+                            }
                     }
+                }
+                gp += kp_bytes(info);
                 if (++since == 8) fold_row();
             }
             ++computed;
             ci += c;
-            if (ci == dc.nkps) {
+            if (++cs == dc.nsteps) {
                 fold_row();
                 // row g + 8(t&1): limbs over the row's four lanes
                 __int128 v0 = ((__int128)acc[0] << (16 * t)) + ((__int128)acc[1] << (16 * t + 8));
@@ -964,7 +988,6 @@ __global__ void __launch_bounds__(kWarps * 32, QH_ROW_CTAS) row_kernel(Arena A, 
                 R += shfl_xor_i128(R, 2);
                 const long long tb = ((long long)cp * n_tiles + dc.tile) * 8;
                 if (t < 2) st_i128(W.plr + (tb + dc.q * dc.H + dc.h) * 16 + g + 8 * t, R);
-                ci = 0;
                 advance();
             }
             __syncwarp();
@@ -1283,6 +1306,7 @@ int upload(Layout&& L, int device, qh_matrix** out) {
     m->A.kp_info = base + S.kp_info;
     m->A.slot_rec = reinterpret_cast<const SlotRec*>(base + S.slot_rec);
     m->A.kpg_cexp = reinterpret_cast<const int32_t*>(base + S.kpg_cexp);
+    m->A.row_steps = reinterpret_cast<const uint32_t*>(base + S.row_steps);
     *out = m;
     return QH_OK;
 }
