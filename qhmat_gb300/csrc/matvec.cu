@@ -606,6 +606,13 @@ __global__ void __launch_bounds__(kWarps * 32, QH_COL_CTAS) column_kernel(Arena 
         int ck = 0, cp = 0, cc = 0;  // compute cursor
         ColTask dc = di;
         const int xe0 = W.xe[0];
+        // this lane's component record (component, scale), loaded when a unit
+        // starts and used at its end
+        int4 rec = make_int4(0, 0, 0, 0);
+        auto load_rec = [&]() {
+            if (lane < dc.count) rec = __ldg(reinterpret_cast<const int4*>(A.task_rec + dc.comp_idx + lane));
+        };
+        load_rec();
         while (ck < nb) {
             issue();
             const unsigned slot_i = computed % kColStages;
@@ -658,7 +665,6 @@ __global__ void __launch_bounds__(kWarps * 32, QH_COL_CTAS) column_kernel(Arena 
                             const longlong2 v = r2[l];
                             S += ((__int128)v.x << (16 * l)) + ((__int128)v.y << (16 * l + 8));
                         }
-                        const int4 rec = __ldg(reinterpret_cast<const int4*>(A.task_rec + dc.comp_idx + lane));
                         W.u[(long long)cp * n_comp + rec.x] =
                             xe ? i128_ldexp(S, xe - 1022 - kFixBits) * __hiloint2double(rec.w, rec.z) : 0.0;
                     }
@@ -682,7 +688,10 @@ __global__ void __launch_bounds__(kWarps * 32, QH_COL_CTAS) column_kernel(Arena 
                 cc = 0;
                 if (++cp == rhs) {
                     cp = 0;
-                    if (++ck < nb) dc = load_task(my_tasks + ck);
+                    if (++ck < nb) {
+                        dc = load_task(my_tasks + ck);
+                        load_rec();
+                    }
                 }
             }
             __syncwarp();
