@@ -1245,8 +1245,10 @@ int upload(Layout&& L, int device, qh_matrix** out) {
     m->device = device;
     cudaDeviceGetAttribute(&m->sms, cudaDevAttrMultiProcessorCount, device);
     {
-        // warp schedules for this device's grids (cost ~ bytes moved plus a
-        // fixed cost per unit)
+        // warp schedules for this device's grids.  Cost model in bytes of
+        // stream: each chunk / k-pair also pays a fixed cost (B fragments,
+        // loop), each unit a finalize and pipeline start worth about three
+        // chunks of the widest tasks (clock64 section timings).
         Layout& Lm = m->L;
         m->col_grid = std::max(1, std::min((Lm.n_tasks + kWarps - 1) / kWarps, m->sms * 2));
         m->row_grid = std::max(1, std::min((Lm.n_units + kWarps - 1) / kWarps, m->sms * 2));
@@ -1256,16 +1258,16 @@ int upload(Layout&& L, int device, qh_matrix** out) {
         std::vector<int32_t> corder, coff, rorder, roff;
         schedule(Lm.n_tasks, m->col_grid * kWarps, [&](int i) {
             const ColTask& T = tasks[i];
-            return double(T.nchunks) * double(T.stride + 512) + 3000.0;
+            return double(T.nchunks) * double(T.stride + 512 + 1024) + 12000.0;
         }, corder, coff);
         schedule(Lm.n_units, m->row_grid * kWarps, [&](int i) {
             const RowUnit& U = units[i];
             double b = 0;
             for (int k = 0; k < U.nkps; ++k) {
                 const int info = kpi[U.kp_off + U.h + int64_t(k) * U.H];
-                b += (info & 7) * 512 - __builtin_popcount(unsigned(info >> 3)) * 256 + 512;
+                b += (info & 7) * 512 - __builtin_popcount(unsigned(info >> 3)) * 256 + 512 + 512;
             }
-            return b + 2000.0;
+            return b + 6000.0;
         }, rorder, roff);
         permute(tasks, corder);
         permute(units, rorder);
