@@ -162,6 +162,16 @@ QH_API int qh_matmul_host(const qh_matrix* m, const double* x, double* y, size_t
  * Used when writing QHMAT001 images. */
 QH_API uint64_t qh_fnv1a64(const void* bytes, size_t len);
 
+/* Dense reconstruction of the represented matrix, the reference's
+ * HMatrix::reconstruct (src/qhmat/core.cpp:392-410) behind HMatrix.to_dense
+ * (python/qhmat/matrix.py:309-311, bindings.cpp:180-190), on the GPU: `out`
+ * receives order x order doubles, row-major in source order (entry (i, k) at
+ * out[i * order + k]); out_on_device != 0 if `out` is device memory.  The
+ * entries equal the reference's bit for bit (same FP64 operations in the
+ * same order).  Synchronises.  Errors: "output size does not match order *
+ * order" (QH_EINVAL), "dense output size overflow" (QH_EOVERFLOW). */
+QH_API int qh_matrix_reconstruct(const qh_matrix* m, double* out, size_t out_count, int out_on_device);
+
 /* Validation aid: decode every stored code of one factor side on the device
  * with the same device routine the apply kernels use, and copy the integers
  * to host `out`, component-major in block order (component c of a block with

@@ -29,12 +29,16 @@ _ref = None
 
 
 def build(force: bool = False) -> Path:
-    """Compile qhmat_oracle.c with the host C compiler (portable C11, -O2)."""
+    """Compile qhmat_oracle.c with the host C compiler (portable C11, -O2).
+
+    -ffp-contract=off keeps every a * b + c as a rounded multiply and a
+    rounded add, as the reference's own x86-64 build evaluates them; aarch64
+    compilers would otherwise fuse them into FMAs and change the last bit."""
     src = HERE / "qhmat_oracle.c"
     if force or not LIB.exists() or LIB.stat().st_mtime < src.stat().st_mtime:
         LIB.parent.mkdir(exist_ok=True)
         tmp = LIB.with_suffix(f".{os.getpid()}.tmp")
-        subprocess.run(["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-fvisibility=hidden",
+        subprocess.run(["gcc", "-O2", "-std=c11", "-ffp-contract=off", "-fPIC", "-shared", "-fvisibility=hidden",
                         "-D_GNU_SOURCE", str(src), "-o", str(tmp), "-lm", "-lpthread"],
                        check=True)
         os.replace(tmp, LIB)

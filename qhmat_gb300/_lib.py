@@ -74,6 +74,8 @@ def load_library() -> C.CDLL:
     lib.qh_fnv1a64.argtypes = [C.c_char_p, sz]
     lib.qh_debug_decode.restype = i32
     lib.qh_debug_decode.argtypes = [vp, i32, vp, sz, C.POINTER(sz)]
+    lib.qh_matrix_reconstruct.restype = i32
+    lib.qh_matrix_reconstruct.argtypes = [vp, vp, sz, i32]
     _lib = lib
     return lib
 

@@ -665,6 +665,8 @@ Layout build_layout(const HostMatrix& m) {
     S.slot_rec = place(sizeof(SlotRec) * slot_rec.size());
     S.kpg_cexp = place(4 * kpg_cexp.size());
     S.row_steps = place(4 * row_steps.size());
+    S.comp_sl = place(8 * C);
+    S.comp_sr = place(8 * C);
     S.total = off;
 
     L.arena.assign(S.total, 0);
@@ -677,6 +679,8 @@ Layout build_layout(const HostMatrix& m) {
         // One rounding: s_P * s_Q.  In exact arithmetic the block contribution
         // sum_j (s_P c_P)(sum_k s_Q c_Q x) equals sum_j c_P (s_P s_Q) sum_k c_Q x.
         at<double>(A, S.comp_s)[c] = m.left_scale[c] * m.right_scale[c];
+        at<double>(A, S.comp_sl)[c] = m.left_scale[c];
+        at<double>(A, S.comp_sr)[c] = m.right_scale[c];
     }
     if (!tasks.empty()) std::memcpy(at<ColTask>(A, S.tasks), tasks.data(), sizeof(ColTask) * tasks.size());
     if (!task_rec.empty()) std::memcpy(A.data() + S.task_rec, task_rec.data(), sizeof(TaskRec) * task_rec.size());

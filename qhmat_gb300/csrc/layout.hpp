@@ -186,7 +186,7 @@ inline bool top_is_nibble(int w) { return w - 8 * (code_planes(w) - 1) <= 4; }
 // Byte offsets of each section inside the device arena.
 struct Sections {
     size_t perm, lr, dd, comp_w, comp_s, tasks, task_rec, qcodes, pcodes, dense, tiles, tdense, units, kp_info,
-        slot_rec, kpg_cexp, row_steps;
+        slot_rec, kpg_cexp, row_steps, comp_sl, comp_sr;
     size_t total;
 };
 

@@ -121,6 +121,8 @@ struct Arena {
     const SlotRec* slot_rec;
     const int32_t* kpg_cexp;
     const uint32_t* row_steps;
+    const double* comp_sl;  // s^P per component
+    const double* comp_sr;  // s^Q per component
 };
 
 struct Work {
@@ -1117,6 +1119,50 @@ __global__ void decode_row_kernel(Arena A, int n_units, const long long* __restr
     }
 }
 
+// Dense reconstruction (src/qhmat/core.cpp:392-410): thread per entry of one
+// block (blocks by binary search over the entry prefix), value = the dense
+// entry or 0, plus, per component in order, (c^P s^P)(c^Q s^Q) with separate
+// IEEE multiplies and adds in the reference's order, written to
+// out[perm[row] * n + perm[col]].  Codes come from decode_*_kernel
+// (component-major: comp_base_l[c] + block row, comp_base_r[c] + block column).
+__global__ void reconstruct_kernel(Arena A, int n_lr, int n_dense, const long long* __restrict__ ent0,
+                                   long long total, const int* __restrict__ lcodes, const int* __restrict__ rcodes,
+                                   const long long* __restrict__ lbase, const long long* __restrict__ rbase,
+                                   int n, double* __restrict__ out) {
+    const int nb = n_lr + n_dense;
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+         e += (long long)gridDim.x * blockDim.x) {
+        int lo = 0, hi = nb - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (ent0[mid] <= e) lo = mid;
+            else hi = mid - 1;
+        }
+        const long long le = e - ent0[lo];
+        double value = 0.0;
+        int row, col;
+        if (lo < n_lr) {
+            const LowRankDesc d = A.lr[lo];
+            const int i = int(le / d.n), k = int(le % d.n);
+            for (int j = 0; j < d.rank; ++j) {
+                const int c = d.comp0 + j;
+                const double l = __dmul_rn(double(lcodes[lbase[c] + i]), A.comp_sl[c]);
+                const double r = __dmul_rn(double(rcodes[rbase[c] + k]), A.comp_sr[c]);
+                value = __dadd_rn(value, __dmul_rn(l, r));
+            }
+            row = d.row0 + i;
+            col = d.col0 + k;
+        } else {
+            const DenseDesc d = A.dd[lo - n_lr];
+            const int i = int(le / d.n), k = int(le % d.n);
+            value = A.dense[d.off + (long long)k * d.m + i];
+            row = d.row0 + i;
+            col = d.col0 + k;
+        }
+        out[(long long)A.perm[row] * n + A.perm[col]] = value;
+    }
+}
+
 // ---------------------------------------------------------------- host side
 
 thread_local std::string g_last_error;
@@ -1318,6 +1364,8 @@ int upload(Layout&& L, int device, qh_matrix** out) {
     m->A.slot_rec = reinterpret_cast<const SlotRec*>(base + S.slot_rec);
     m->A.kpg_cexp = reinterpret_cast<const int32_t*>(base + S.kpg_cexp);
     m->A.row_steps = reinterpret_cast<const uint32_t*>(base + S.row_steps);
+    m->A.comp_sl = reinterpret_cast<const double*>(base + S.comp_sl);
+    m->A.comp_sr = reinterpret_cast<const double*>(base + S.comp_sr);
     *out = m;
     return QH_OK;
 }
@@ -1673,6 +1721,89 @@ int qh_matmul_host(const qh_matrix* m, const double* x, double* y, size_t rhs) {
     if (*mm->h_status & kStatusTimeout) return fail(QH_ERUNTIME, "device copy wait timed out");
     std::memcpy(y, mm->pinned, vec);
     return QH_OK;
+}
+
+int qh_matrix_reconstruct(const qh_matrix* m, double* out, size_t out_count, int out_on_device) {
+    if (!m) return fail(QH_EINVAL, "null matrix handle");
+    const size_t n = m->L.order;
+    if (n > SIZE_MAX / n / sizeof(double)) return fail(QH_EOVERFLOW, "dense output size overflow");
+    if (!out || out_count != n * n) return fail(QH_EINVAL, "output size does not match order * order");
+    return guarded([&] {
+        DeviceGuard g(m->device);
+        int rc = QH_OK;
+        const int n_lr = m->L.n_lr, n_dense = m->L.n_dense, nb = n_lr + n_dense;
+        std::vector<LowRankDesc> lr(static_cast<size_t>(n_lr));
+        std::vector<DenseDesc> dd(static_cast<size_t>(n_dense));
+        cudaError_t e = cudaSuccess;
+        if (n_lr) e = cudaMemcpy(lr.data(), m->A.lr, sizeof(LowRankDesc) * lr.size(), cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess && n_dense)
+            e = cudaMemcpy(dd.data(), m->A.dd, sizeof(DenseDesc) * dd.size(), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy device-to-host");
+        // code offsets (component-major, as qh_debug_decode lays them out) and
+        // the entry prefix of the blocks
+        std::vector<long long> lbase(size_t(m->L.n_comp) + 1, 0), rbase(size_t(m->L.n_comp) + 1, 0);
+        for (const auto& d : lr)
+            for (int j = 0; j < d.rank; ++j) {
+                lbase[size_t(d.comp0 + j) + 1] = d.m;
+                rbase[size_t(d.comp0 + j) + 1] = d.n;
+            }
+        for (size_t c = 0; c + 1 < lbase.size(); ++c) {
+            lbase[c + 1] += lbase[c];
+            rbase[c + 1] += rbase[c];
+        }
+        const long long ltotal = lbase.back(), rtotal = rbase.back();
+        std::vector<long long> lrow(lbase);  // left codes are indexed by clustered row
+        for (const auto& d : lr)
+            for (int j = 0; j < d.rank; ++j) lrow[size_t(d.comp0 + j)] -= d.row0;
+        std::vector<long long> ent0(size_t(nb) + 1, 0);
+        for (int b = 0; b < nb; ++b) {
+            const long long mm = b < n_lr ? lr[size_t(b)].m : dd[size_t(b - n_lr)].m;
+            const long long nn = b < n_lr ? lr[size_t(b)].n : dd[size_t(b - n_lr)].n;
+            ent0[size_t(b) + 1] = ent0[size_t(b)] + mm * nn;
+        }
+        const long long total = ent0[size_t(nb)];
+        // device scratch: codes, offsets, entry prefix, and the output if on the host
+        std::vector<void*> bufs;
+        auto alloc = [&](size_t bytes) -> void* {
+            void* p = nullptr;
+            if (cudaMalloc(&p, std::max<size_t>(bytes, 16)) != cudaSuccess) return nullptr;
+            bufs.push_back(p);
+            return p;
+        };
+        auto* d_lc = static_cast<int*>(alloc(4 * size_t(ltotal)));
+        auto* d_rc = static_cast<int*>(alloc(4 * size_t(rtotal)));
+        auto* d_lb = static_cast<long long*>(alloc(8 * lbase.size()));
+        auto* d_lr = static_cast<long long*>(alloc(8 * lbase.size()));
+        auto* d_rb = static_cast<long long*>(alloc(8 * rbase.size()));
+        auto* d_e0 = static_cast<long long*>(alloc(8 * ent0.size()));
+        double* d_out = out_on_device ? out : static_cast<double*>(alloc(8 * n * n));
+        if (!d_lc || !d_rc || !d_lb || !d_lr || !d_rb || !d_e0 || !d_out) {
+            for (void* p : bufs) cudaFree(p);
+            return fail(QH_ERUNTIME, "cudaMalloc: out of device memory");
+        }
+        e = cudaMemcpy(d_lb, lbase.data(), 8 * lbase.size(), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(d_lr, lrow.data(), 8 * lrow.size(), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(d_rb, rbase.data(), 8 * rbase.size(), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(d_e0, ent0.data(), 8 * ent0.size(), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemset(d_out, 0, 8 * n * n);
+        if (e == cudaSuccess) {
+            if (m->L.n_tasks)
+                decode_col_kernel<<<std::max(1, std::min((m->L.n_tasks + 7) / 8, 4096)), 256>>>(m->A, m->L.n_tasks,
+                                                                                              d_rb, d_rc);
+            if (m->L.n_units)
+                decode_row_kernel<<<std::max(1, std::min((m->L.n_units + 7) / 8, 4096)), 256>>>(m->A, m->L.n_units,
+                                                                                              d_lr, d_lc);
+            if (total)
+                reconstruct_kernel<<<unsigned(std::min<long long>((total + 255) / 256, 65536)), 256>>>(
+                    m->A, n_lr, n_dense, d_e0, total, d_lc, d_rc, d_lb, d_rb, int(n), d_out);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = cudaDeviceSynchronize();
+        if (e == cudaSuccess && !out_on_device) e = cudaMemcpy(out, d_out, 8 * n * n, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) rc = cuda_fail(e, "reconstruct");
+        for (void* p : bufs) cudaFree(p);
+        return rc;
+    });
 }
 
 int qh_debug_decode(const qh_matrix* m, int side, int32_t* out, size_t out_count, size_t* needed) {

@@ -189,6 +189,15 @@ class HMatrix:
     def __matmul__(self, x):
         return self.matmul(x)
 
+    def to_dense(self) -> np.ndarray:
+        """The represented matrix as a dense FP64 array in source order, built on
+        the GPU; equal bit for bit to ``qhmat.HMatrix.to_dense``
+        (python/qhmat/matrix.py:309-311)."""
+        n = self.order
+        out = np.empty((n, n), np.float64)
+        raise_for(self._lib.qh_matrix_reconstruct(self._h, out.ctypes.data, out.size, 0))
+        return out
+
     def debug_decode(self, side: int) -> np.ndarray:
         """All codes of one factor side decoded on the GPU (component-major)."""
         need = C.c_size_t()
@@ -205,6 +214,11 @@ class NativeHMatrix(HMatrix):
         if not use_cuda:
             raise RuntimeError("qhmat_gb300 applies on the GPU only; pass use_cuda=True")
         return super().matmul(x, device="cuda", **kw)
+
+    def reconstruct(self) -> np.ndarray:
+        """``NativeHMatrix.reconstruct()`` (src/qhmat/bindings.cpp:180-190): the
+        dense matrix, flattened row-major."""
+        return self.to_dense().reshape(-1)
 
 
 def cuda_built() -> bool:

@@ -147,3 +147,20 @@ def test_from_arrays_matches_file_path(cuda_device):
                             np.concatenate(rw), loff, roff, ls, rs, widths)
     ref = HMatrix.from_bytes(data)
     assert np.array_equal(h.matmul(g["x"]), ref.matmul(g["x"]))
+
+
+@pytest.mark.parametrize("name", [n for n in GOLDEN_CASES if n not in ("ragged300", "cfg1")])
+def test_to_dense_bit_exact(cuda_device, name):
+    """GPU reconstruct == the reference's HMatrix::reconstruct, bit for bit."""
+    data, g = golden(name)
+    h = HMatrix.from_bytes(data)
+    dense = h.to_dense()
+    assert dense.shape == (h.order, h.order)
+    np.testing.assert_array_equal(dense, g["dense"])
+    np.testing.assert_array_equal(NativeHMatrix.from_bytes(data).reconstruct(), g["dense"].reshape(-1))
+
+
+def test_to_dense_matches_oracle_reconstruct(cuda_device):
+    data, _ = golden("ragged300")
+    h = HMatrix.from_bytes(data)
+    np.testing.assert_array_equal(h.to_dense(), O.OracleMatrix(data).reconstruct())
