@@ -484,7 +484,7 @@ Layout build_layout(const HostMatrix& m) {
     int64_t n_slots = 0;
     std::vector<TileDense> tdense;
     std::vector<SlotRec> slot_rec;   // each B row slot's component, split row and width
-    std::vector<int32_t> kpg_cexp;   // exponent offset of each B row group's tile
+    std::vector<std::vector<std::pair<int32_t, int32_t>>> comp_dest(m.width.size());  // per component: (slot, tile)
     std::vector<uint32_t> row_steps; // pipeline steps of the row units
     struct RowComp {
         int w;
@@ -516,36 +516,26 @@ Layout build_layout(const HostMatrix& m) {
             const int32_t K = int32_t(kc.size());
             const int32_t Kp = (K + 31) / 32;
             T.qrows = (rows + 15) / 16;
-            T.hsplit = T.qrows == 1 ? 8 : (T.qrows == 2 ? 4 : 2);
+            T.hsplit = kTileUnits / T.qrows;
             T.nh = std::min(T.hsplit, Kp);
             T.c_exp = kNoExp;
             for (const auto& c : kc) T.c_exp = std::max(T.c_exp, beta[size_t(c.comp)]);
             const int64_t kp_off = int64_t(kp_info.size());
-            // per k-pair: planes and nibble planes
-            std::vector<int> kplanes(static_cast<size_t>(Kp), 0), knib(static_cast<size_t>(Kp), 0);
+            // per k-pair (widths non-increasing along k): the planes and top
+            // digit bits of its widest code; narrower codes are written on
+            // the same planes (sign-extended)
+            std::vector<int> kplanes(static_cast<size_t>(Kp), 0), knib(static_cast<size_t>(Kp), 0),
+                ktop(static_cast<size_t>(Kp), 0);
             for (int32_t kp = 0; kp < Kp; ++kp) {
-                int planes = 0, nibs = 0;
-                for (int mm = 0; mm < 4; ++mm) {
-                    bool any = false, all_nib = true;
-                    for (int32_t k = 32 * kp; k < std::min(K, 32 * kp + 32); ++k) {
-                        const int w = kc[size_t(k)].w;
-                        if (code_planes(w) > mm) {
-                            any = true;
-                            if (!(code_planes(w) == mm + 1 && top_is_nibble(w))) all_nib = false;
-                        }
-                    }
-                    if (any) {
-                        planes = mm + 1;
-                        if (all_nib) nibs |= 1 << mm;
-                    }
-                }
+                const int w = kc[size_t(32 * kp)].w;
+                const int planes = code_planes(w), tb = w - 8 * (planes - 1);
                 kplanes[size_t(kp)] = planes;
-                knib[size_t(kp)] = nibs;
-                kp_info.push_back(uint8_t(planes | (nibs << 3)));
+                knib[size_t(kp)] = top_is_nibble(w) ? 1 << (planes - 1) : 0;
+                ktop[size_t(kp)] = tb;
+                kp_info.push_back(uint8_t(planes | (top_is_nibble(w) ? 8 : 0) | ((tb - 1) << 4)));
             }
             // B row slots: k split h's k-pairs contiguously
             std::vector<int64_t> hslot(size_t(T.hsplit), 0);
-            T.kpg0 = int32_t(n_slots / 32);
             for (int32_t h = 0; h < T.nh; ++h) {
                 hslot[size_t(h)] = n_slots;
                 for (int32_t kp = h; kp < Kp; kp += T.hsplit) {
@@ -554,15 +544,14 @@ Layout build_layout(const HostMatrix& m) {
                         if (k < K) {
                             const int32_t c = kc[size_t(k)].comp;
                             slot_rec.push_back({c, ((comp_part[size_t(c)] + 1) << 8) | int32_t(m.width[size_t(c)])});
+                            comp_dest[size_t(c)].push_back({int32_t(slot_rec.size() - 1), ti});
                         } else {
                             slot_rec.push_back({-1, 1});
                         }
                     }
-                    kpg_cexp.push_back(T.c_exp);
                 }
                 n_slots += 32 * int64_t((Kp - h + T.hsplit - 1) / T.hsplit);
             }
-            T.nkpg = int32_t(n_slots / 32) - T.kpg0;
             // streams (q, h): groups of 16 rows
             for (int32_t q = 0; q < T.qrows; ++q)
                 for (int32_t h = 0; h < T.nh; ++h) {
@@ -599,6 +588,8 @@ Layout build_layout(const HostMatrix& m) {
                     for (int32_t kp = h; kp < Kp; kp += T.hsplit)
                         for (int mm = 0; mm < kplanes[size_t(kp)]; ++mm) {
                             const bool nb = (knib[size_t(kp)] >> mm) & 1;
+                            const bool top = mm == kplanes[size_t(kp)] - 1;
+                            const int64_t half = int64_t(1) << (ktop[size_t(kp)] - 1);
                             const size_t rb = nb ? 16 : 32;
                             const size_t g0 = pcodes.size();
                             pcodes.resize(g0 + 16 * rb, 0);
@@ -613,8 +604,9 @@ Layout build_layout(const HostMatrix& m) {
                                     const auto& b = m.blocks[size_t(c.block)];
                                     const uint32_t* run = m.left_words.data() + m.left_off[size_t(c.comp)];
                                     const uint64_t br = r + uint64_t(tr) - b.row0;
-                                    const uint32_t u = offset_code(code_of(run, br, c.w), c.w);
-                                    put_digit(row, nb, e >> 4, e & 15, (u >> (8 * mm)) & (nb ? 15u : 255u));
+                                    const int64_t code = code_of(run, br, c.w);
+                                    const int64_t d = top ? (code >> (8 * mm)) + half : (code >> (8 * mm)) & 255;
+                                    put_digit(row, nb, e >> 4, e & 15, uint32_t(d) & (nb ? 15u : 255u));
                                 }
                             }
                             bytes += int64_t(16 * rb);
@@ -631,7 +623,66 @@ Layout build_layout(const HostMatrix& m) {
     std::vector<RowUnit> unit_list;
     for (const auto& u : units) unit_list.push_back(u.second);
     L.n_tiles = int32_t(tiles.size());
-    L.n_kpg = int32_t(kpg_cexp.size());
+    for (const auto& R : tiles)
+        if (R.c_exp < -32768 || R.c_exp > 32767) throw overflow_error("row tile exponent out of range");
+    // per column task: the B rows its components feed (component row << 24)
+    std::vector<TaskDest> task_dest;
+    for (auto& T : tasks) {
+        if (T.part == 0 || T.nparts == 1) {
+            T.dest0 = int32_t(task_dest.size());
+            std::vector<std::pair<int32_t, TaskDest>> lst;  // (tile, record)
+            for (int32_t r = 0; r < T.count; ++r)
+                for (const auto& [slot, ti] : comp_dest[size_t(task_rec[size_t(T.comp_idx + r)].comp)]) {
+                    const int32_t ce = tiles[size_t(ti)].c_exp;
+                    lst.push_back({ti, {slot, (r << 16) | int32_t(uint16_t(int16_t(ce)))}});
+                }
+            std::stable_sort(lst.begin(), lst.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
+            for (const auto& e : lst) task_dest.push_back(e.second);
+            T.ndest = int32_t(task_dest.size()) - T.dest0;
+        }
+    }
+    // parts of a split task share its list
+    {
+        std::vector<std::pair<int32_t, int32_t>> by_split(size_t(n_split), {0, 0});
+        for (const auto& T : tasks)
+            if (T.nparts > 1 && T.part == 0) by_split[size_t(T.split_id)] = {T.dest0, T.ndest};
+        for (auto& T : tasks)
+            if (T.nparts > 1) {
+                T.dest0 = by_split[size_t(T.split_id)].first;
+                T.ndest = by_split[size_t(T.split_id)].second;
+            }
+    }
+    {
+        size_t fed = 0;
+        for (const auto& v : comp_dest) fed += v.size();
+        if (fed != task_dest.size()) throw runtime_error("internal: a row-side B row has no column task");
+    }
+    L.n_dest = int32_t(task_dest.size());
+    // dense diagonal blocks: column-side units of kDenseCols columns of one
+    // block part of a row tile (width 0), each with its own row-sum slice
+    int32_t n_dslices = 0;
+    for (size_t ti = 0; ti < tiles.size(); ++ti) {
+        RowTile& R = tiles[ti];
+        R.ds0 = n_dslices;
+        for (int32_t j = 0; j < R.ndense; ++j) {
+            const TileDense& D = tdense[size_t(R.dense0 + j)];
+            for (int32_t k0 = 0; k0 < D.cols; k0 += kDenseCols) {
+                ColTask T{};
+                T.col0 = R.dense0 + j;
+                T.chunk0 = k0;
+                T.n = std::min(kDenseCols, D.cols - k0);
+                T.stride = int32_t(ti);
+                T.comp_idx = n_dslices++;
+                T.nparts = 1;
+                T.split_id = -1;
+                T.cps = 1;
+                tasks.push_back(T);
+            }
+        }
+        R.nds = n_dslices - R.ds0;
+    }
+    L.n_dslices = n_dslices;
+    L.n_tasks = int32_t(tasks.size());
     L.n_units = int32_t(unit_list.size());
     L.n_slots = int32_t(n_slots);
     L.n_tdense = int32_t(tdense.size());
@@ -663,7 +714,7 @@ Layout build_layout(const HostMatrix& m) {
     S.units = place(sizeof(RowUnit) * unit_list.size());
     S.kp_info = place(kp_info.size() + 16);
     S.slot_rec = place(sizeof(SlotRec) * slot_rec.size());
-    S.kpg_cexp = place(4 * kpg_cexp.size());
+    S.task_dest = place(sizeof(TaskDest) * task_dest.size());
     S.row_steps = place(4 * row_steps.size());
     S.comp_sl = place(8 * C);
     S.comp_sr = place(8 * C);
@@ -689,7 +740,7 @@ Layout build_layout(const HostMatrix& m) {
     if (!kp_info.empty()) std::memcpy(A.data() + S.kp_info, kp_info.data(), kp_info.size());
     if (!unit_list.empty()) std::memcpy(A.data() + S.units, unit_list.data(), sizeof(RowUnit) * unit_list.size());
     if (!slot_rec.empty()) std::memcpy(A.data() + S.slot_rec, slot_rec.data(), sizeof(SlotRec) * slot_rec.size());
-    if (!kpg_cexp.empty()) std::memcpy(A.data() + S.kpg_cexp, kpg_cexp.data(), 4 * kpg_cexp.size());
+    if (!task_dest.empty()) std::memcpy(A.data() + S.task_dest, task_dest.data(), sizeof(TaskDest) * task_dest.size());
     if (!row_steps.empty()) std::memcpy(A.data() + S.row_steps, row_steps.data(), 4 * row_steps.size());
     if (!dense_cm.empty()) std::memcpy(A.data() + S.dense, dense_cm.data(), 8 * dense_cm.size());
     if (!tiles.empty()) std::memcpy(A.data() + S.tiles, tiles.data(), sizeof(RowTile) * tiles.size());

@@ -6,13 +6,17 @@
 // on the CPU.
 //
 // Codes are stored as digit planes laid out for the tensor cores.  A code c of
-// width w (two's complement) is offset to u = c + 2^(w-1) in [0, 2^w) and cut
-// into P = ceil(w/8) base-256 digits d_m = (u >> 8m) & 255; the top digit
-// holds t = w - 8(P-1) bits and is stored as a nibble when t <= 4.  Then
-//     sum_i c_i v_i = sum_m 2^(8m) sum_i d_m,i v_i  -  2^(w-1) sum_i v_i,
-// and every inner sum is an exact small-integer product sum (digits <= 255
-// times 8-bit limbs of the fixed-point operand), which the f16 tensor-core
-// MMA computes exactly in FP32 (no partial sum reaches 2^24).  Digits are
+// width w (two's complement) on P = ceil(w/8) planes with t = w - 8(P-1) top
+// bits is
+//     c = sum_{m<P-1} 2^(8m) d_m + 2^(8(P-1)) (d_top - 2^(t-1)),
+// d_m = (c >> 8m) & 255 and d_top = (c >> 8(P-1)) + 2^(t-1) in [0, 2^t)
+// (stored as a nibble when t <= 4).  The device reads the top digit as the
+// signed d_top - 2^(t-1), so
+//     sum_i c_i v_i = sum_m 2^(8m) sum_i digit_m,i v_i
+// with no offset correction, and every inner sum is an exact small-integer
+// product sum (|digits| <= 255 times 8-bit limbs of the fixed-point operand),
+// which the f16 tensor-core MMA computes exactly in FP32 (no partial sum
+// reaches 2^24).  Digits are
 // grouped into the 16x16 A-operand fragments of mma.m16n8k16: within a
 // 16-entry k-block, thread t of a fragment row needs entries 2t, 2t+1, 2t+8,
 // 2t+9, and those four digits are stored together:
@@ -24,19 +28,19 @@
 //  * right factor Q (column side): components sharing a column range and a
 //    width form tasks of <= 32 (two 16-row M-tiles).  Per 32-entry chunk a
 //    task stores, for each M-tile q and plane m, the group of its rows_q rows;
-//    entries past the range hold code 0.  The device reads the top digit as
-//    signed (d = stored - 2^(t-1)), so the column side needs no correction.
+//    entries past the range hold code 0.
 //  * left factor P (row side): rows are cut into tiles of <= 64 rows inside
 //    one elementary row slab.  The components of all blocks covering a tile
-//    are sorted by width and form the tile's k axis (k-pairs of 32).  The
-//    tile's M-tile q (16 rows) and k split h own one contiguous stream (a row
-//    unit): for every k-pair kp = h, h + H, ... and every plane m of the
-//    k-pair, one group of 16 rows (zero past the tile or past the k axis).
-//    Each k slot has a B row, written for every apply: the eight f16 limbs of
-//    U = u in fixed point on the tile's exponent; a unit's B rows are
-//    contiguous (slot = tile base + h's base + 32 i + lane for its i-th
-//    k-pair), and every 32 slots (a B row group) also get the sum of
-//    2^(w-1) U that corrects the offset codes.
+//    are sorted by width, widest first, and form the tile's k axis (k-pairs
+//    of 32).  A k-pair's codes are all written on the planes of its widest
+//    code (P and t of that width; narrower codes sign-extended).  The tile's
+//    M-tile q (16 rows) and k split h own one contiguous stream (a row unit):
+//    for every k-pair kp = h, h + H, ... and every plane m of the k-pair, one
+//    group of 16 rows (zero past the tile or past the k axis).  Each k slot
+//    has a B row, written for every apply by the column task that computes
+//    its component: the eight f16 limbs of U = u in fixed point on the tile's
+//    exponent; a unit's B rows are contiguous (slot = tile base + h's base +
+//    32 i + lane for its i-th k-pair).
 //  * dense diagonal blocks are stored column-major (value (i, k) at
 //    off + k*m + i) so that lanes owning consecutive rows read consecutive
 //    doubles.
@@ -89,8 +93,11 @@ HostMatrix parse_qhmat(const uint8_t* bytes, size_t len);
 // rectangles, ranks, widths, finite values, partition cover).
 void validate(const HostMatrix& m);
 
-// Rows of one row tile at most (one CTA of the row-side kernel).
+// Rows of one row tile at most.
 constexpr int kTileRows = 64;
+// Row units of one tile at most: its M-tiles (16 rows each) times the k
+// splits, hsplit = kTileUnits / M-tiles.
+constexpr int kTileUnits = 8;
 // Entries of one column-side chunk (one code per lane per entry).
 constexpr int kColChunk = 32;
 // x entries per exponent chunk of the fixed-point right-hand side.
@@ -112,7 +119,11 @@ struct LowRankDesc {
 // rows of 32 bytes (16 for a nibble top plane).  A pipeline step carries
 // `cps` chunks.  A task longer than kMaxPartChunks chunks is split into
 // `nparts` parts whose partial sums are combined by the part that finishes
-// last.
+// last.  The task's components feed ndest row-side B rows, listed at
+// task_dest[dest0 ..] (every part holds the same list; the finishing part
+// writes them).  A unit of width 0 instead holds columns [chunk0, chunk0 + n)
+// of the dense diagonal block part tdense[col0] of row tile `stride`, its row
+// sums going to dense slice comp_idx.
 struct ColTask {
     int32_t col0, n, count, width;
     int64_t off;
@@ -121,8 +132,15 @@ struct ColTask {
     int32_t part, nparts;
     int32_t split_id;           // index of the split task (counter / partials), -1 if nparts == 1
     int32_t cps;
-    int32_t pad[2];
+    int32_t dest0, ndest;
 };
+// A row-side B row fed by a column task: slot, and (component row in the
+// task) << 16 | the tile's exponent offset as a 16-bit signed field.  A task's
+// list is ordered by (tile, row), so that a tile's B rows are consecutive.
+struct TaskDest {
+    int32_t slot, row_cexp;
+};
+static_assert(sizeof(TaskDest) == 8, "TaskDest layout");
 static_assert(sizeof(ColTask) == 64, "ColTask layout");
 // Finalize operands of one component of a column task (one 16-byte load).
 struct TaskRec {
@@ -135,13 +153,14 @@ struct DenseDesc {
 };
 // One row tile: clustered rows [row0, row0 + rows) inside one slab; qrows
 // M-tiles, k axis split hsplit ways (nh of the splits have k-pairs); dense
-// blocks tdense[dense0 .. dense0 + ndense); B row groups (32 slots each)
-// kpg0 .. kpg0 + nkpg - 1; u is put in fixed point on the exponent field
-// xe + c_exp (xe: the largest exponent field of x).
+// blocks tdense[dense0 .. dense0 + ndense), whose row sums are kept as dense
+// slices ds0 .. ds0 + nds - 1 (kDenseCols columns each, in column order); u
+// is put in fixed point on the exponent field xe + c_exp (xe: the largest
+// exponent field of x).
 struct RowTile {
     int32_t row0, rows, qrows, hsplit;
     int32_t nh, ndense, dense0, c_exp;
-    int32_t kpg0, nkpg, pad[2];
+    int32_t ds0, nds, pad[2];
 };
 static_assert(sizeof(RowTile) == 48, "RowTile layout");
 // A dense diagonal block's part in a row tile: value (tile row r, column k)
@@ -176,6 +195,8 @@ constexpr int kColSlotBytes = 4608;
 constexpr int kRowSlotBytes = 4096;
 // Longest run of chunks one column unit walks.
 constexpr int kMaxPartChunks = 16;
+// Columns of a dense block in one column-side dense unit (one slice).
+constexpr int kDenseCols = 16;
 // Exponent offset of a row tile without nonzero components.
 constexpr int32_t kNoExp = -4000;
 
@@ -185,8 +206,8 @@ inline bool top_is_nibble(int w) { return w - 8 * (code_planes(w) - 1) <= 4; }
 
 // Byte offsets of each section inside the device arena.
 struct Sections {
-    size_t perm, lr, dd, comp_w, comp_s, tasks, task_rec, qcodes, pcodes, dense, tiles, tdense, units, kp_info,
-        slot_rec, kpg_cexp, row_steps, comp_sl, comp_sr;
+    size_t perm, lr, dd, comp_w, comp_s, tasks, task_rec, task_dest, qcodes, pcodes, dense, tiles, tdense, units,
+        kp_info, slot_rec, row_steps, comp_sl, comp_sr;
     size_t total;
 };
 
@@ -194,7 +215,7 @@ struct Layout {
     uint64_t order = 0;
     int32_t n_lr = 0, n_dense = 0, n_comp = 0, n_tiles = 0, n_chunks = 0;
     int32_t n_tasks = 0, n_split = 0, max_parts = 1;
-    int32_t n_units = 0, n_slots = 0, n_tdense = 0, n_kpg = 0;
+    int32_t n_units = 0, n_slots = 0, n_tdense = 0, n_dest = 0, n_dslices = 0;
     std::vector<uint8_t> arena;  // host image of the device arena
     Sections sec{};
     double bound = 0;

@@ -17,13 +17,13 @@
 //                      rhs column; X = round(x 2^(62-e)) as eight f16 limbs.
 //   column_kernel      warp per task (<= 32 components sharing a column range
 //                      and a width): t_j = sum_i c_ij X_i exactly, then
-//                      u_j = (s^P s^Q) t_j 2^(e-1022-62) in FP64.
-//   expand_kernel      u of each row tile's components in fixed point on the
-//                      tile's exponent (a layout-time bound), as limb rows;
-//                      plus the dense diagonal blocks in FP64.
+//                      u_j = (s^P s^Q) t_j 2^(e-1022-62) in FP64, then u in
+//                      fixed point on each consuming row tile's exponent (a
+//                      layout-time bound) as that tile's B rows (limbs).
 //   row_kernel         warp per (row tile, 16 rows, k split): sum_j c_ij U_j
 //                      exactly, stored as 128-bit partial sums.
-//   combine_kernel     thread per row: partials -> y (one conversion).
+//   combine_kernel     CTA per row tile: the dense diagonal blocks in FP64,
+//                      plus the partials -> y (one conversion).
 //
 // The only rounding steps are the fixed-point conversions of x and u (2^-63
 // of the column's largest |x|, of the tile's bound on |u|), the product
@@ -119,7 +119,7 @@ struct Arena {
     const RowUnit* units;
     const uint8_t* kp_info;
     const SlotRec* slot_rec;
-    const int32_t* kpg_cexp;
+    const TaskDest* task_dest;
     const uint32_t* row_steps;
     const double* comp_sl;  // s^P per component
     const double* comp_sr;  // s^Q per component
@@ -130,18 +130,13 @@ struct Work {
     int* xblk;         // [rhs][nblk]         largest exponent field of x per prep block
     int* xe;           // [rhs]               largest exponent field of x
     uint4* xq;         // [rhs][n_pad]        limbs of X (zero past n)
-    double* u;         // [rhs][n_comp]       u_j = (s^P s^Q) sum_i c_ij x_i (unsplit tasks)
     long long* lsplit; // [rhs][n_split*33][8] per-limb sums sum_i c_ij limb_l(X_i) of split tasks'
                        //                     components (rows split_id*33 + j; zeroed by prep)
+    int* split_cnt;    // [rhs][n_split]      finished parts of each split task (zeroed by prep)
     uint4* blimb;      // [rhs][n_slots]      row-side B rows: limbs of U
-    uint4* kpbias;     // [rhs][n_kpg]        sum of 2^(w-1) U over each B row group (128-bit)
-    uint4* plr;        // [rhs][n_tiles][8][16] low-rank row sums of each row unit (128-bit)
-    double* pdense;    // [rhs][n_tiles][kDenseSlices][64] dense diagonal row sums per column slice
+    uint4* plr;        // [rhs][n_tiles][kTileUnits][16] low-rank row sums of each row unit (128-bit)
+    double* pdense;    // [rhs][n_dslices][64] dense diagonal row sums per dense slice
 };
-
-// Column slices a tile's dense diagonal blocks are cut into (one thread per
-// row and slice in expand_kernel; summed in slice order by combine_kernel).
-constexpr int kDenseSlices = 8;
 
 // -------------------------------------------------- bulk copies (TMA)
 
@@ -158,23 +153,22 @@ __device__ __forceinline__ void mbar_arrive_expect(uint64_t* bar, unsigned bytes
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes)
                  : "memory");
 }
-// Potentially blocking test of a phase: the thread is suspended until the
-// phase completes or kSuspendNs nanoseconds pass, so that a waiting warp does
-// not spin on the issue slots the computing warps need.
-constexpr unsigned kSuspendNs = 1000000u;
+// Potentially blocking test of a phase: the thread waits until the phase
+// completes or a system-dependent time limit passes (measured faster than an
+// explicit suspend-time hint, which delays the wake-up).
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
     unsigned ok;
     asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
         : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity), "r"(kSuspendNs)
+        : "r"(smem_u32(bar)), "r"(parity)
         : "memory");
     return ok != 0;
 }
-// Bounded wait: gives up (returns false) after kWaitLimit tests (at most about
-// kWaitLimit * kSuspendNs) instead of hanging; callers record the failure in
-// the status word and stop.
-constexpr int kWaitLimit = 2048;
+// Bounded wait: gives up (returns false) after kWaitLimit tests (seconds at
+// most) instead of hanging; callers record the failure in the status word and
+// stop.
+constexpr int kWaitLimit = 1 << 22;
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
     for (int i = 0; i < kWaitLimit; ++i)
         if (mbar_try_wait(bar, parity)) return true;
@@ -214,6 +208,8 @@ constexpr int kColStages = QH_COL_STAGES;
 constexpr int kRowStages = QH_ROW_STAGES;
 constexpr int kWarps = 8;
 constexpr int kColPipeSmem = kWarps * kColStages * kColSlotBytes;
+// Unit descriptors a column warp keeps in shared memory.
+constexpr int kStagedUnits = 24;
 constexpr int kRowPipeSmem = kWarps * kRowStages * kRowSlotBytes;
 
 // Status bits written by the kernels (status word of the apply).
@@ -353,6 +349,30 @@ __device__ __forceinline__ void group_mma_top(float (&d)[4], const uint8_t* grp,
     }
 }
 
+// The top plane of a row k-pair: stored digits s = d + 2^(t-1) become the
+// signed digit d on the lower planes' scale, d 2^-24 (a subnormal f16 for
+// |d| < 1024): the f16 with exponent field 1 and mantissa s is (1024 + s)
+// 2^-24, minus hb = (1024 + 2^(t-1)) 2^-24 in both halves, exactly.
+__device__ __forceinline__ uint32_t rtop_lo(uint32_t w, uint32_t hb) { return hsub2(prmt(w, 0x04040404u, 0x4140u), hb); }
+__device__ __forceinline__ uint32_t rtop_hi(uint32_t w, uint32_t hb) { return hsub2(prmt(w, 0x04040404u, 0x4342u), hb); }
+__device__ __forceinline__ uint32_t rtop_nib(uint32_t v, int k, uint32_t hb) {
+    return hsub2(nib_pair(v, k) | 0x04000400u, hb);
+}
+__device__ __forceinline__ void group_mma_rtop(float (&d)[4], const uint8_t* grp, bool nib, int g, int t,
+                                               const uint32_t (&b)[4], uint32_t hb) {
+    if (nib) {
+        const uint32_t v0 = *reinterpret_cast<const uint32_t*>(grp + g * 16 + 4 * t);
+        const uint32_t v1 = *reinterpret_cast<const uint32_t*>(grp + (g + 8) * 16 + 4 * t);
+        mma_dig(d, rtop_nib(v0, 0, hb), rtop_nib(v1, 0, hb), rtop_nib(v0, 1, hb), rtop_nib(v1, 1, hb), b[0], b[1]);
+        mma_dig(d, rtop_nib(v0, 2, hb), rtop_nib(v1, 2, hb), rtop_nib(v0, 3, hb), rtop_nib(v1, 3, hb), b[2], b[3]);
+    } else {
+        const uint2 w0 = *reinterpret_cast<const uint2*>(grp + g * 32 + 8 * t);
+        const uint2 w1 = *reinterpret_cast<const uint2*>(grp + (g + 8) * 32 + 8 * t);
+        mma_dig(d, rtop_lo(w0.x, hb), rtop_lo(w1.x, hb), rtop_hi(w0.x, hb), rtop_hi(w1.x, hb), b[0], b[1]);
+        mma_dig(d, rtop_lo(w0.y, hb), rtop_lo(w1.y, hb), rtop_hi(w0.y, hb), rtop_hi(w1.y, hb), b[2], b[3]);
+    }
+}
+
 // Digits of rows g, g+8 of a group as integers, in the order the MMA sees
 // them (for validation): out[half][kb*4 + s], s = entries 2t, 2t+1, 2t+8, 2t+9.
 __device__ __forceinline__ void group_digits(const uint8_t* grp, bool nib, int rows, int g, int t,
@@ -456,17 +476,24 @@ __global__ void __launch_bounds__(256) x_limbs_kernel(Work W, int n, int n_pad, 
 
 // Bring a line into L1 ahead of its use (no register waits on it).
 __device__ __forceinline__ void prefetch_l1(const void* p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
+__device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+// 8-byte asynchronous global -> shared copy (no register held while in flight).
+__device__ __forceinline__ void cp_async8(void* dst, const void* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 // A column unit's descriptor (four 16-byte loads, cached in L1).
-__device__ __forceinline__ ColTask load_task(const ColTask* p) {
-    const int4* q = reinterpret_cast<const int4*>(p);
-    const int4 a = __ldg(q), b = __ldg(q + 1), c = __ldg(q + 2), d = __ldg(q + 3);
+// A column unit's descriptor from four 16-byte words (shared or global).
+__device__ __forceinline__ ColTask load_task(const int4* q) {
+    const int4 a = q[0], b = q[1], c = q[2], d = q[3];
     ColTask T;
     T.col0 = a.x, T.n = a.y, T.count = a.z, T.width = a.w;
     T.off = (long long)(((unsigned long long)(unsigned)b.y << 32) | (unsigned)b.x);
     T.stride = b.z, T.comp_idx = b.w;
     T.chunk0 = c.x, T.nchunks = c.y, T.part = c.z, T.nparts = c.w;
     T.split_id = d.x, T.cps = d.y;
+    T.dest0 = d.z, T.ndest = d.w;
     return T;
 }
 
@@ -527,6 +554,31 @@ __device__ __forceinline__ void col_step(ColAcc& a, const uint8_t* slot, int nc,
     }
 }
 
+// A dense unit of the column side: columns [k0, k0 + nc) of a dense diagonal
+// block part of one row tile for rhs column p, lane l owning tile rows l and
+// l + 32 (columns in order, FP64; consecutive lanes read consecutive doubles),
+// stored as the unit's row-sum slice.  The FP64 pipe is the scarce one on
+// this GPU, so the blocks are cut into many short units that spread over all
+// schedulers and run beside the other warps' integer and tensor-core work.
+__device__ __forceinline__ void dense_unit(const Arena& A, const Work& W, const ColTask& u, int p, int n,
+                                           int n_dslices, int lane) {
+    const int rows = __ldg(&A.tiles[u.stride].rows);
+    const TileDense D = A.tdense[u.col0];
+    const bool r0 = lane < rows, r1 = lane + 32 < rows;
+    const double* col = A.dense + D.off + (long long)u.chunk0 * D.ld + lane;
+    const double* xv = W.xc + (long long)p * n + D.xcol + u.chunk0;
+    double s0 = 0.0, s1 = 0.0;
+#pragma unroll 4
+    for (int k = 0; k < u.n; ++k) {
+        const double xk = __ldcg(xv + k);
+        if (r0) s0 = fma(__ldg(col + (long long)k * D.ld), xk, s0);
+        if (r1) s1 = fma(__ldg(col + (long long)k * D.ld + 32), xk, s1);
+    }
+    double* out = W.pdense + ((long long)p * n_dslices + u.comp_idx) * 64;
+    out[lane] = s0;
+    out[lane + 32] = s1;
+}
+
 // Column side.  Warp gw owns the units warp_off[gw] .. warp_off[gw + 1]
 // (assigned longest first at upload, heaviest first per warp); its work
 // is the sequence (unit, rhs column, chunk), streamed through a kColStages-deep
@@ -540,10 +592,12 @@ __device__ __forceinline__ void col_step(ColAcc& a, const uint8_t* slot, int nc,
 // and lane (g, t) converts component 16(t>>1) + 8(t&1) + g to
 // u_j = (s^P s^Q) t_j 2^(xe - 1022 - kFixBits).
 __global__ void __launch_bounds__(kWarps * 32, QH_COL_CTAS) column_kernel(Arena A, Work W, const int* __restrict__ warp_off,
-                                                                int n_pad, int rhs, int n_comp, int n_split,
-                                                                int* status) {
+                                                                int n_pad, int rhs, int n_split, int n_slots,
+                                                                int n, int n_dslices, int* status) {
     extern __shared__ __align__(16) uint8_t smem_raw[];
     __shared__ __align__(8) uint64_t s_bar[kWarps][kColStages];
+    __shared__ int2 s_td[kWarps][32];  // each lane's first B row record of the current unit
+    __shared__ int4 s_desc[kWarps][kStagedUnits * 4];  // the warp's first unit descriptors
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int g = lane >> 2, t = lane & 3;
     uint8_t* slots = smem_raw + (size_t)warp * kColStages * kColSlotBytes;
@@ -556,6 +610,20 @@ __global__ void __launch_bounds__(kWarps * 32, QH_COL_CTAS) column_kernel(Arena 
     const int gw = blockIdx.x * kWarps + warp;
     const int u0 = __ldg(warp_off + gw), my_units = __ldg(warp_off + gw + 1) - u0;
     const ColTask* my_tasks = A.tasks + u0;
+    // the warp's first kStagedUnits descriptors into shared memory (read-only
+    // layout: before waiting for the preceding kernel)
+    {
+        const int4* src = reinterpret_cast<const int4*>(my_tasks);
+        const int nst = min(my_units, kStagedUnits) * 4;
+        for (int i = lane; i < nst; i += 32) s_desc[warp][i] = __ldg(src + i);
+        __syncwarp();
+    }
+    auto unit = [&](int k) {
+        if (k < kStagedUnits) return load_task(&s_desc[warp][4 * k]);
+        const int4* q = reinterpret_cast<const int4*>(my_tasks + k);
+        const int4 gq[4] = {__ldg(q), __ldg(q + 1), __ldg(q + 2), __ldg(q + 3)};
+        return load_task(gq);
+    };
     if (my_units <= 0) pdl_wait();  // (every thread waits before exiting)
     unsigned issued = 0, computed = 0;  // running step counters (slot, phase)
     ColAcc a;
@@ -572,9 +640,12 @@ __global__ void __launch_bounds__(kWarps * 32, QH_COL_CTAS) column_kernel(Arena 
     if (my_units > 0) {
         const int nb = my_units;
         int ik = 0, ip = 0, ic = 0;  // issue cursor
-        ColTask di = load_task(my_tasks);
+        ColTask di = unit(0);
         pdl_wait();  // x limbs and exponents of this apply
         auto issue = [&]() {
+            while (ik < nb && di.width == 0) {  // dense units stream nothing
+                if (++ik < nb) di = unit(ik);
+            }
             if (ik >= nb) return;
             const int nc = min(di.cps, di.nchunks - ic);
             const unsigned slot_i = issued % kColStages;
@@ -595,27 +666,39 @@ __global__ void __launch_bounds__(kWarps * 32, QH_COL_CTAS) column_kernel(Arena 
                 if (++ip == rhs) {
                     ip = 0;
                     if (++ik < nb) {
-                        di = load_task(my_tasks + ik);
-                        if (ik + 2 < nb && lane == 0) prefetch_l1(my_tasks + ik + 2);
+                        di = unit(ik);
                     }
                 }
             }
         };
-        if (lane < 2 && lane + 1 < nb) prefetch_l1(my_tasks + lane + 1);
         __syncwarp();
+        int ck = 0, cp = 0, cc = 0;  // compute cursor (first unit: before the issue cursor moves on)
+        ColTask dc = di;
 #pragma unroll 1
         for (int s = 0; s < kColStages - 1; ++s) issue();
-        int ck = 0, cp = 0, cc = 0;  // compute cursor
-        ColTask dc = di;
         const int xe0 = W.xe[0];
-        // this lane's component record (component, scale), loaded when a unit
-        // starts and used at its end
-        int4 rec = make_int4(0, 0, 0, 0);
+        // this lane's component scale and first B row record, loaded when a
+        // unit starts (the record by an asynchronous copy into shared
+        // memory) and used at its end
+        double rec = 0.0;
+        int2* my_td = &s_td[warp][lane];
         auto load_rec = [&]() {
-            if (lane < dc.count) rec = __ldg(reinterpret_cast<const int4*>(A.task_rec + dc.comp_idx + lane));
+            if (lane < dc.count) rec = __ldg(&A.task_rec[dc.comp_idx + lane].scale);
+            if (lane < dc.ndest) cp_async8(my_td, A.task_dest + dc.dest0 + lane);
         };
         load_rec();
         while (ck < nb) {
+            if (dc.width == 0) {  // dense unit: no stage
+                dense_unit(A, W, dc, cp, n, n_dslices, lane);
+                if (++cp == rhs) {
+                    cp = 0;
+                    if (++ck < nb) {
+                        dc = unit(ck);
+                        load_rec();
+                    }
+                }
+                continue;
+            }
             issue();
             const unsigned slot_i = computed % kColStages;
             if (!mbar_wait(bar + slot_i, (computed / kColStages) & 1)) {
@@ -646,10 +729,12 @@ __global__ void __launch_bounds__(kWarps * 32, QH_COL_CTAS) column_kernel(Arena 
                 // this lane's per-limb sums: rows 16q + g + 8h, limbs 2t, 2t+1.
                 // Unsplit task: stage all rows' sums in the consumed slot (not
                 // refilled before the next issue) and let lane j finish row j;
-                // a part of a split task adds its sums exactly with atomics.
+                // a part of a split task adds its sums exactly with atomics and
+                // the part that finishes last finishes the rows.
                 const int xe = cp == 0 ? xe0 : W.xe[cp];
+                long long* st = reinterpret_cast<long long*>(const_cast<uint8_t*>(slot));
+                bool finish = true;
                 if (dc.nparts == 1) {
-                    long long* st = reinterpret_cast<long long*>(const_cast<uint8_t*>(slot));
 #pragma unroll
                     for (int q = 0; q < 2; ++q)
 #pragma unroll
@@ -658,7 +743,40 @@ __global__ void __launch_bounds__(kWarps * 32, QH_COL_CTAS) column_kernel(Arena 
                             *reinterpret_cast<longlong2*>(st + row * 8 + 2 * t) =
                                 make_longlong2(a.acc[q][2 * hh], a.acc[q][2 * hh + 1]);
                         }
+                } else {
+                    long long* blk = W.lsplit + ((long long)cp * n_split * 33 + dc.split_id * 33) * 8;
+#pragma unroll
+                    for (int q = 0; q < 2; ++q)
+#pragma unroll
+                        for (int hh = 0; hh < 2; ++hh) {
+                            const int row = 16 * q + 8 * hh + g;
+                            if (row >= dc.count) continue;
+                            unsigned long long* dst = reinterpret_cast<unsigned long long*>(blk + row * 8 + 2 * t);
+                            atomicAdd(dst, (unsigned long long)a.acc[q][2 * hh]);
+                            atomicAdd(dst + 1, (unsigned long long)a.acc[q][2 * hh + 1]);
+                        }
+                    __threadfence();
                     __syncwarp();
+                    int done = 0;
+                    if (lane == 0) done = atomicAdd(W.split_cnt + (long long)cp * n_split + dc.split_id, 1);
+                    done = __shfl_sync(0xFFFFFFFFu, done, 0);
+                    finish = done == dc.nparts - 1;
+                    if (finish) {
+                        __threadfence();
+                        if (lane < dc.count) {
+                            const longlong2* src = reinterpret_cast<const longlong2*>(blk + lane * 8);
+#pragma unroll
+                            for (int l = 0; l < 4; ++l)
+                                *reinterpret_cast<longlong2*>(st + lane * 8 + 2 * l) = __ldcg(src + l);
+                        }
+                    }
+                }
+                if (finish) {
+                    for (int l = 32 + 16 * lane; l < dc.ndest; l += 512)  // the rest of a long B row list
+                        prefetch_l2(A.task_dest + dc.dest0 + l);
+                    __syncwarp();
+                    // lane j: u of component row j
+                    double u = 0.0;
                     if (lane < dc.count) {
                         const longlong2* r2 = reinterpret_cast<const longlong2*>(st + lane * 8);
                         __int128 S = 0;
@@ -667,21 +785,30 @@ __global__ void __launch_bounds__(kWarps * 32, QH_COL_CTAS) column_kernel(Arena 
                             const longlong2 v = r2[l];
                             S += ((__int128)v.x << (16 * l)) + ((__int128)v.y << (16 * l + 8));
                         }
-                        W.u[(long long)cp * n_comp + rec.x] =
-                            xe ? i128_ldexp(S, xe - 1022 - kFixBits) * __hiloint2double(rec.w, rec.z) : 0.0;
+                        u = xe ? i128_ldexp(S, xe - 1022 - kFixBits) * rec : 0.0;
                     }
-                } else {
+                    // the task's B rows, lanes over the (component, slot)
+                    // pairs: U on the tile's exponent and its limbs
+                    const int2* tdp = reinterpret_cast<const int2*>(A.task_dest + dc.dest0);
+                    cp_async_wait_all();  // this lane's first record
+                    for (int d0 = 0; d0 < dc.ndest; d0 += 128) {
+                        int2 td[4];
 #pragma unroll
-                    for (int q = 0; q < 2; ++q)
-#pragma unroll
-                        for (int hh = 0; hh < 2; ++hh) {
-                            const int row = 16 * q + 8 * hh + g;
-                            if (row >= dc.count) continue;
-                            unsigned long long* dst = reinterpret_cast<unsigned long long*>(
-                                W.lsplit + ((long long)cp * n_split * 33 + dc.split_id * 33 + row) * 8 + 2 * t);
-                            atomicAdd(dst, (unsigned long long)a.acc[q][2 * hh]);
-                            atomicAdd(dst + 1, (unsigned long long)a.acc[q][2 * hh + 1]);
+                        for (int j = 0; j < 4; ++j) {
+                            const int d = d0 + 32 * j + lane;
+                            td[j] = d < dc.ndest ? (d0 + j == 0 ? *my_td : __ldg(tdp + d)) : make_int2(-1, 0);
                         }
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) {
+                            if (d0 + 32 * j >= dc.ndest) break;
+                            const double ud = __shfl_sync(0xFFFFFFFFu, u, (td[j].y >> 16) & 31);
+                            if (td[j].x >= 0) {
+                                const int ce = int(int16_t(td[j].y & 0xFFFF));
+                                const long long U = to_fixed(ud, xe + ce);  // (0 for 0)
+                                W.blimb[(long long)cp * n_slots + td[j].x] = to_limbs(U);
+                            }
+                        }
+                    }
                 }
 #pragma unroll
                 for (int q = 0; q < 2; ++q)
@@ -691,7 +818,7 @@ __global__ void __launch_bounds__(kWarps * 32, QH_COL_CTAS) column_kernel(Arena 
                 if (++cp == rhs) {
                     cp = 0;
                     if (++ck < nb) {
-                        dc = load_task(my_tasks + ck);
+                        dc = unit(ck);
                         load_rec();
                     }
                 }
@@ -706,71 +833,10 @@ __global__ void __launch_bounds__(kWarps * 32, QH_COL_CTAS) column_kernel(Arena 
     }
 }
 
-// Bytes of a row k-pair's digit groups (kp_info: planes | nibble planes << 3).
-__device__ __forceinline__ int kp_bytes(int info) {
-    const int planes = info & 7, nibs = info >> 3;
-    return planes * 512 - __popc(nibs) * 256;
-}
-
-// B rows of the row side: one warp per group of 32 slots (one k-pair of a
-// row unit).  Lane l takes u of the slot's component (formed here from the
-// per-limb sums for a split task), puts it in fixed point on the tile's
-// exponent and stores its limbs; the group's offset correction
-// sum 2^(w-1) U is reduced over the warp.
-__global__ void __launch_bounds__(256) expand_kernel(Arena A, Work W, int n, int n_kpg, int n_slots, int n_comp,
-                                                     int n_split, int n_tiles, int rhs, int kpg_blocks) {
-    pdl_trigger();
-    pdl_wait();
-    const int lane = threadIdx.x & 31;
-    if ((int)blockIdx.x >= kpg_blocks) {
-        // dense diagonal blocks: CTA per (tile, rhs column), thread per
-        // (column slice, row); columns of a slice in order
-        const int b = int(blockIdx.x) - kpg_blocks;  // two CTAs per (tile, rhs column)
-        const int p = (b >> 1) / n_tiles, tile = (b >> 1) % n_tiles;
-        const int sl = (b & 1) * 4 + (threadIdx.x >> 6), r = threadIdx.x & 63;
-        const RowTile T = A.tiles[tile];
-        double dg = 0.0;
-        if (r < T.rows) {
-            for (int bb = 0; bb < T.ndense; ++bb) {
-                const TileDense D = A.tdense[T.dense0 + bb];
-                const int k0 = D.cols * sl / kDenseSlices, k1 = D.cols * (sl + 1) / kDenseSlices;
-                const double* col = A.dense + D.off + r;
-                const double* xv = W.xc + (long long)p * n + D.xcol;
-                for (int k = k0; k < k1; ++k) dg = fma(__ldg(col + (long long)k * D.ld), __ldg(xv + k), dg);
-            }
-        }
-        W.pdense[(((long long)p * n_tiles + tile) * kDenseSlices + sl) * 64 + r] = dg;
-        return;
-    }
-    const long long gw = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    if (gw >= (long long)n_kpg * rhs) return;
-    const int p = int(gw / n_kpg), kpg = int(gw % n_kpg);
-    const int slot = kpg * 32 + lane;
-    const int2 rec = __ldg(reinterpret_cast<const int2*>(A.slot_rec + slot));
-    const int ce = __ldg(A.kpg_cexp + kpg);
-    const int xe = W.xe[p];
-    const int c = rec.x, w = rec.y & 255, pr = (rec.y >> 8) - 1;
-    long long U = 0;
-    if (c >= 0) {
-        double uv;
-        if (pr < 0) {
-            uv = W.u[(long long)p * n_comp + c];
-        } else {
-            // split task: t_c = sum_l 2^(8l) (per-limb sums of all parts), exactly
-            const long long* ls = W.lsplit + ((long long)p * n_split * 33 + pr) * 8;
-            __int128 S = 0;
-#pragma unroll
-            for (int l = 0; l < 8; ++l) S += (__int128)__ldcg(ls + l) << (8 * l);
-            uv = xe ? i128_ldexp(S, xe - 1022 - kFixBits) * __ldg(A.comp_s + c) : 0.0;
-        }
-        if (uv != 0.0) U = to_fixed(uv, xe + ce);
-    }
-    W.blimb[(long long)p * n_slots + slot] = to_limbs(U);
-    __int128 b = (__int128)U << (c >= 0 ? w - 1 : 0);
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) b += shfl_xor_i128(b, o);
-    if (lane == 0) st_i128(W.kpbias + (long long)p * n_kpg + kpg, b);
-}
+// A row k-pair's info byte: planes | nibble top plane << 3 | (top bits - 1) << 4.
+// Bytes of its digit groups, and the top plane's conversion constant.
+__device__ __forceinline__ int kp_bytes(int info) { return (info & 7) * 512 - ((info >> 3) & 1) * 256; }
+__device__ __forceinline__ uint32_t kp_hb(int info) { return (0x0400u | (1u << (info >> 4))) * 0x00010001u; }
 
 // A row unit's descriptor (four 16-byte loads, cached in L1).
 struct RowDesc {
@@ -793,13 +859,14 @@ __device__ __forceinline__ RowDesc load_rdesc(const RowUnit* p) {
 // The digit groups of one k-pair with P planes (nibble top plane if NIBTOP),
 // at compile-time offsets.
 template <int P, bool NIBTOP>
-__device__ __forceinline__ void kp_groups(float (&D)[4][4], const uint8_t* gp, int g, int t, const uint32_t (&b)[4]) {
+__device__ __forceinline__ void kp_groups(float (&D)[4][4], const uint8_t* gp, int g, int t, const uint32_t (&b)[4],
+                                          uint32_t hb) {
 #pragma unroll
-    for (int m = 0; m < P; ++m) {
-        const bool nib = NIBTOP && m == P - 1;
-        group_mma(D[m], gp, nib, 16, g, t, b);
-        gp += nib ? 256 : 512;
+    for (int m = 0; m < P - 1; ++m) {
+        group_mma(D[m], gp, false, 16, g, t, b);
+        gp += 512;
     }
+    group_mma_rtop(D[P - 1], gp, NIBTOP, g, t, b, hb);
 }
 
 // Row side.  Warp gw owns the units warp_off[gw] .. warp_off[gw + 1]
@@ -888,12 +955,12 @@ __global__ void __launch_bounds__(kWarps * 32, QH_ROW_CTAS) row_kernel(Arena A, 
             }
         };
         __syncwarp();
-#pragma unroll 1
-        for (int s = 0; s < kRowStages - 1; ++s) issue();
         // compute cursor: unit ck, rhs column cp, step cs (words csb ..), k-pair
-        // index ci (infos cib ..)
+        // index ci (infos cib ..); first unit: before the issue cursor moves on
         int ck = 0, cp = 0, cs = 0, csb = 0, ci = 0, cib = 0;
         RowDesc dc = di;
+#pragma unroll 1
+        for (int s = 0; s < kRowStages - 1; ++s) issue();
         uint32_t csteps = load_steps(dc, 0);
         int cinfo = load_info(dc, 0);
         float D[4][4];
@@ -962,24 +1029,16 @@ __global__ void __launch_bounds__(kWarps * 32, QH_ROW_CTAS) row_kernel(Arena A, 
                         if (e + 1 >= kv) b[i] &= 0x0000FFFFu;
                     }
                 }
-                switch (info) {  // planes | nibble planes << 3: the widths 32, 24, 16, 12, 8, 4
-                    case 4: kp_groups<4, false>(D, gp, g, t, b); break;
-                    case 3: kp_groups<3, false>(D, gp, g, t, b); break;
-                    case 2: kp_groups<2, false>(D, gp, g, t, b); break;
-                    case 2 | (2 << 3): kp_groups<2, true>(D, gp, g, t, b); break;
-                    case 1: kp_groups<1, false>(D, gp, g, t, b); break;
-                    case 1 | (1 << 3): kp_groups<1, true>(D, gp, g, t, b); break;
-                    default: {
-                        const int planes = info & 7, nibs = info >> 3;
-                        const uint8_t* q = gp;
-#pragma unroll
-                        for (int m = 0; m < 4; ++m)
-                            if (m < planes) {
-                                const bool nib = (nibs >> m) & 1;
-                                group_mma(D[m], q, nib, 16, g, t, b);
-                                q += nib ? 256 : 512;
-                            }
-                    }
+                const uint32_t hb = kp_hb(info);
+                switch (info & 15) {  // planes | nibble top << 3
+                    case 4: kp_groups<4, false>(D, gp, g, t, b, hb); break;
+                    case 4 | 8: kp_groups<4, true>(D, gp, g, t, b, hb); break;
+                    case 3: kp_groups<3, false>(D, gp, g, t, b, hb); break;
+                    case 3 | 8: kp_groups<3, true>(D, gp, g, t, b, hb); break;
+                    case 2: kp_groups<2, false>(D, gp, g, t, b, hb); break;
+                    case 2 | 8: kp_groups<2, true>(D, gp, g, t, b, hb); break;
+                    case 1: kp_groups<1, false>(D, gp, g, t, b, hb); break;
+                    default: kp_groups<1, true>(D, gp, g, t, b, hb); break;
                 }
                 gp += kp_bytes(info);
                 if (++since == 8) fold_row();
@@ -997,7 +1056,7 @@ __global__ void __launch_bounds__(kWarps * 32, QH_ROW_CTAS) row_kernel(Arena A, 
                 __int128 R = hi ? v1 : v0;
                 R += shfl_xor_i128(hi ? v0 : v1, 1);
                 R += shfl_xor_i128(R, 2);
-                const long long tb = ((long long)cp * n_tiles + dc.tile) * 8;
+                const long long tb = ((long long)cp * n_tiles + dc.tile) * kTileUnits;
                 if (t < 2) st_i128(W.plr + (tb + dc.q * dc.H + dc.h) * 16 + g + 8 * t, R);
                 advance();
             }
@@ -1012,35 +1071,27 @@ __global__ void __launch_bounds__(kWarps * 32, QH_ROW_CTAS) row_kernel(Arena A, 
 }
 
 // One CTA of 64 threads per (row tile, rhs column), one thread per row: y =
-// the dense diagonal row (its column slices' sums in order) + the low-rank
-// row sums minus the tile's offset correction (reduced by each warp from the
-// B row groups), converted once.
-__global__ void __launch_bounds__(64) combine_kernel(Arena A, Work W, double* __restrict__ y, int n, int n_tiles,
-                                                     int n_kpg, int rhs) {
+// the tile's dense slices (column side) added in column order + the low-rank
+// row sums of the tile's units, converted once.
+__global__ void __launch_bounds__(64) combine_kernel(Arena A, Work W, double* __restrict__ y, int n_tiles,
+                                                    int n_dslices, int rhs) {
     pdl_trigger();
-    const int lane = threadIdx.x & 31, r = threadIdx.x;
-    const int p = blockIdx.y, tile = blockIdx.x;
+    const int p = blockIdx.y, tile = blockIdx.x, r = threadIdx.x;
     const RowTile T = A.tiles[tile];
-    const int rr = r < T.rows ? r : 0;
-    const int out = __ldg(A.perm + T.row0 + rr);
+    if (r >= T.rows) {
+        pdl_wait();
+        return;
+    }
+    const int out = __ldg(A.perm + T.row0 + r);
     pdl_wait();
     const int xe = W.xe[p];
-    // every load depends only on the tile: issue them together
-    const long long tb = ((long long)p * n_tiles + tile) * 8;
+    const long long tb = ((long long)p * n_tiles + tile) * kTileUnits;
     __int128 R = 0;
-    for (int h = 0; h < T.nh; ++h) R += ld_i128(W.plr + (tb + (rr >> 4) * T.hsplit + h) * 16 + (rr & 15));
-    double dg = 0.0;
-    const double* pd = W.pdense + ((long long)p * n_tiles + tile) * kDenseSlices * 64 + rr;
-#pragma unroll
-    for (int sl = 0; sl < kDenseSlices; ++sl) dg += __ldcg(pd + sl * 64);
-    __int128 bias = 0;
-    for (int k = lane; k < T.nkpg; k += 32) bias += ld_i128(W.kpbias + (long long)p * n_kpg + T.kpg0 + k);
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) bias += shfl_xor_i128(bias, o);
-    if (r >= T.rows) return;
-    R -= bias;
+    for (int h = 0; h < T.nh; ++h) R += ld_i128(W.plr + (tb + (r >> 4) * T.hsplit + h) * 16 + (r & 15));
+    double d = 0.0;
+    for (int i = 0; i < T.nds; ++i) d += __ldcg(W.pdense + ((long long)p * n_dslices + T.ds0 + i) * 64 + r);
     const double lr = (xe && T.c_exp != kNoExp) ? i128_ldexp(R, xe + T.c_exp - 1022 - kFixBits) : 0.0;
-    y[(long long)out * rhs + p] = dg + lr;
+    y[(long long)out * rhs + p] = d + lr;
 }
 
 // Validation: decode every code from the resident layout through the same
@@ -1052,6 +1103,7 @@ __global__ void decode_col_kernel(Arena A, int n_tasks, const long long* __restr
     const int warps = gridDim.x * (blockDim.x >> 5);
     for (int ti = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); ti < n_tasks; ti += warps) {
         const ColTask T = A.tasks[ti];
+        if (T.width == 0) continue;  // dense unit
         const int P = (T.width + 7) / 8;
         const bool nibtop = T.width - 8 * (P - 1) <= 4;
         const int RB = (P - 1) * 32 + (nibtop ? 16 : 32);
@@ -1094,14 +1146,15 @@ __global__ void decode_row_kernel(Arena A, int n_units, const long long* __restr
         for (int i = 0; i < U.nkps; ++i) {
             const int kp = U.h + i * U.H;
             const int info = A.kp_info[U.kp_off + kp];
-            const int planes = info & 7, nibs = info >> 3;
-            uint32_t u[2][8] = {};
+            const int planes = info & 7, half = 1 << (info >> 4);
+            long long u[2][8] = {};
             for (int m = 0; m < planes; ++m) {
-                const bool nib = (nibs >> m) & 1;
+                const bool nib = m == planes - 1 && ((info >> 3) & 1);
                 uint32_t d[2][8];
                 group_digits(gp, nib, 16, g, t, d);
                 for (int hh = 0; hh < 2; ++hh)
-                    for (int k = 0; k < 8; ++k) u[hh][k] |= d[hh][k] << (8 * m);
+                    for (int k = 0; k < 8; ++k)
+                        u[hh][k] += (m == planes - 1 ? (long long)d[hh][k] - half : (long long)d[hh][k]) << (8 * m);
                 gp += nib ? 256 : 512;
             }
             for (int hh = 0; hh < 2; ++hh) {
@@ -1111,8 +1164,7 @@ __global__ void decode_row_kernel(Arena A, int n_units, const long long* __restr
                     const int e = slot_entry(k >> 2, k & 3, t);
                     const int c = A.slot_rec[U.slot0 + 32 * i + e].comp;
                     if (c < 0) continue;
-                    const int w = A.comp_w[c];
-                    out[comp_base[c] + T.row0 + tr] = int(int64_t(u[hh][k]) - (int64_t(1) << (w - 1)));
+                    out[comp_base[c] + T.row0 + tr] = int(u[hh][k]);
                 }
             }
         }
@@ -1291,10 +1343,8 @@ int upload(Layout&& L, int device, qh_matrix** out) {
     m->device = device;
     cudaDeviceGetAttribute(&m->sms, cudaDevAttrMultiProcessorCount, device);
     {
-        // warp schedules for this device's grids.  Cost model in bytes of
-        // stream: each chunk / k-pair also pays a fixed cost (B fragments,
-        // loop), each unit a finalize and pipeline start worth about three
-        // chunks of the widest tasks (clock64 section timings).
+        // warp schedules for this device's grids: units longest first, each
+        // to the warp with the least predicted time.
         Layout& Lm = m->L;
         m->col_grid = std::max(1, std::min((Lm.n_tasks + kWarps - 1) / kWarps, m->sms * 2));
         m->row_grid = std::max(1, std::min((Lm.n_units + kWarps - 1) / kWarps, m->sms * 2));
@@ -1303,17 +1353,28 @@ int upload(Layout&& L, int device, qh_matrix** out) {
         const uint8_t* kpi = Lm.arena.data() + Lm.sec.kp_info;
         std::vector<int32_t> corder, coff, rorder, roff;
         schedule(Lm.n_tasks, m->col_grid * kWarps, [&](int i) {
+            // SM cycles of a column unit with all warps resident (least
+            // squares over clock64 timings of every unit of a 32768-point
+            // kernel matrix, R^2 0.97): per unit (descriptor loads, the
+            // finalize), per pipeline step (copy latency not hidden by two
+            // stages), per chunk and per code byte; per 32 B rows written
+            // (timed alone), charged to every part of a split task since any
+            // of them may be the one that finishes it
             const ColTask& T = tasks[i];
-            return double(T.nchunks) * double(T.stride + 512 + 1024) + 12000.0;
+            if (T.width == 0) return 1000.0 * double(T.n);  // dense unit: FP64, ~16k cycles for 16 columns
+            const double steps = double((T.nchunks + T.cps - 1) / T.cps);
+            return 4100.0 + 1415.0 * steps + 490.0 * T.nchunks + 0.194 * double(T.nchunks) * T.stride +
+                   700.0 * double((T.ndest + 31) / 32) + (T.nparts > 1 ? 584.0 : 0.0);
         }, corder, coff);
         schedule(Lm.n_units, m->row_grid * kWarps, [&](int i) {
+            // SM cycles of a row unit with all warps resident (clock64
+            // timings of every unit of a 32768-point kernel matrix): per
+            // k-pair and per digit plane of it (MMAs, digit conversion), per
+            // pipeline step, per unit (descriptor, the 128-bit epilogue)
             const RowUnit& U = units[i];
-            double b = 0;
-            for (int k = 0; k < U.nkps; ++k) {
-                const int info = kpi[U.kp_off + U.h + int64_t(k) * U.H];
-                b += (info & 7) * 512 - __builtin_popcount(unsigned(info >> 3)) * 256 + 512 + 512;
-            }
-            return b + 6000.0;
+            double planes = 0;
+            for (int k = 0; k < U.nkps; ++k) planes += kpi[U.kp_off + U.h + int64_t(k) * U.H] & 7;
+            return 2000.0 + 350.0 * U.nkps + 380.0 * planes + 300.0 * U.nsteps;
         }, rorder, roff);
         permute(tasks, corder);
         permute(units, rorder);
@@ -1362,7 +1423,7 @@ int upload(Layout&& L, int device, qh_matrix** out) {
     m->A.tdense = reinterpret_cast<const TileDense*>(base + S.tdense);
     m->A.kp_info = base + S.kp_info;
     m->A.slot_rec = reinterpret_cast<const SlotRec*>(base + S.slot_rec);
-    m->A.kpg_cexp = reinterpret_cast<const int32_t*>(base + S.kpg_cexp);
+    m->A.task_dest = reinterpret_cast<const TaskDest*>(base + S.task_dest);
     m->A.row_steps = reinterpret_cast<const uint32_t*>(base + S.row_steps);
     m->A.comp_sl = reinterpret_cast<const double*>(base + S.comp_sl);
     m->A.comp_sr = reinterpret_cast<const double*>(base + S.comp_sr);
@@ -1386,7 +1447,7 @@ int guarded(F&& f) {
 }
 
 struct WsPlan {
-    size_t xc, xblk, xe, xq, u, lsplit, blimb, kpbias, plr, pdense, total;
+    size_t xc, xblk, xe, xq, lsplit, cnt, blimb, plr, pdense, total, zero0, zero_bytes;
     int nblk;
 };
 
@@ -1402,16 +1463,18 @@ WsPlan ws_plan(const Layout& L, size_t rhs) {
         return o;
     };
     w.nblk = (L.n_chunks + 7) / 8;
-    w.lsplit = take(8 * 8 * 33 * size_t(L.n_split) * rhs);  // zeroed by prep_x
+    // zeroed by prep_x (contiguous): split partial sums and counters
+    w.zero0 = off;
+    w.lsplit = take(8 * 8 * 33 * size_t(L.n_split) * rhs);
+    w.cnt = take(4 * size_t(L.n_split) * rhs);
+    w.zero_bytes = off - w.zero0;
     w.xe = take(4 * rhs);
     w.xblk = take(4 * size_t(w.nblk) * rhs);
     w.xc = take(8 * L.order * rhs);
     w.xq = take(16 * padded_order(L) * rhs);
-    w.u = take(8 * size_t(L.n_comp) * rhs);
     w.blimb = take(16 * size_t(L.n_slots) * rhs);
-    w.kpbias = take(16 * size_t(L.n_kpg) * rhs);
-    w.plr = take(16 * 16 * 8 * size_t(L.n_tiles) * rhs);
-    w.pdense = take(8 * 64 * kDenseSlices * size_t(L.n_tiles) * rhs);
+    w.plr = take(16 * 16 * kTileUnits * size_t(L.n_tiles) * rhs);
+    w.pdense = take(8 * 64 * size_t(L.n_dslices) * rhs);
     w.total = off;
     return w;
 }
@@ -1446,10 +1509,9 @@ int launch(const qh_matrix* m, const double* x, double* y, size_t rhs, void* ws,
     W.xblk = reinterpret_cast<int*>(w + P.xblk);
     W.xe = reinterpret_cast<int*>(w + P.xe);
     W.xq = reinterpret_cast<uint4*>(w + P.xq);
-    W.u = reinterpret_cast<double*>(w + P.u);
     W.lsplit = reinterpret_cast<long long*>(w + P.lsplit);
+    W.split_cnt = reinterpret_cast<int*>(w + P.cnt);
     W.blimb = reinterpret_cast<uint4*>(w + P.blimb);
-    W.kpbias = reinterpret_cast<uint4*>(w + P.kpbias);
     W.plr = reinterpret_cast<uint4*>(w + P.plr);
     W.pdense = reinterpret_cast<double*>(w + P.pdense);
     auto mark = [&](int i) {
@@ -1458,27 +1520,22 @@ int launch(const qh_matrix* m, const double* x, double* y, size_t rhs, void* ws,
     const int irhs = int(rhs);
     mark(0);
     prep_x_kernel<<<dim3(unsigned(P.nblk), unsigned(rhs)), 256, 0, s>>>(
-        m->A, W, x, n, irhs, L.n_chunks, reinterpret_cast<int*>(W.lsplit), L.n_split * 33 * 8 * 2 * irhs, status);
+        m->A, W, x, n, irhs, L.n_chunks, reinterpret_cast<int*>(w + P.zero0), int(P.zero_bytes / 4), status);
     const int n_pad = int(padded_order(L));
     cudaError_t e = launch_pdl(x_limbs_kernel, dim3(unsigned((n_pad + 255) / 256), unsigned(rhs)), dim3(256), 0, s,
                                W, n, n_pad, P.nblk);
     mark(1);
     if (e == cudaSuccess && L.n_tasks > 0)
         e = launch_pdl(column_kernel, dim3(unsigned(m->col_grid)), dim3(kWarps * 32), size_t(kColPipeSmem), s, m->A,
-                       W, static_cast<const int*>(m->sched), n_pad, irhs, L.n_comp, L.n_split, status);
-    if (e == cudaSuccess) {
-        const int kpg_blocks = int(((long long)L.n_kpg * irhs + 7) / 8);
-        e = launch_pdl(expand_kernel, dim3(unsigned(kpg_blocks + 2 * L.n_tiles * irhs)), dim3(256), 0, s, m->A, W, n,
-                       L.n_kpg, L.n_slots, L.n_comp, L.n_split, L.n_tiles, irhs, kpg_blocks);
-    }
+                       W, static_cast<const int*>(m->sched), n_pad, irhs, L.n_split, L.n_slots, n, L.n_dslices, status);
     mark(2);
     if (e == cudaSuccess && L.n_units > 0)
         e = launch_pdl(row_kernel, dim3(unsigned(m->row_grid)), dim3(kWarps * 32), size_t(kRowPipeSmem), s, m->A, W,
                        static_cast<const int*>(m->sched + m->col_grid * kWarps + 1), irhs, L.n_slots, L.n_tiles,
                        status);
     if (e == cudaSuccess)
-        e = launch_pdl(combine_kernel, dim3(unsigned(L.n_tiles), unsigned(rhs)), dim3(64), 0, s, m->A, W, y, n,
-                       L.n_tiles, L.n_kpg, irhs);
+        e = launch_pdl(combine_kernel, dim3(unsigned(L.n_tiles), unsigned(rhs)), dim3(64), 0, s, m->A, W, y,
+                       L.n_tiles, L.n_dslices, irhs);
     if (e != cudaSuccess) return cuda_fail(e, "CUDA kernel launch");
     mark(3);
     e = cudaGetLastError();
