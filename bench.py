@@ -359,13 +359,13 @@ def main():
             rw += inf["right_words"]
     n = h.order
     comps = st["components"]
-    # phases: prep (x gathered, exponent, limbs), column (column kernel, which
-    # also writes the row side's B rows), row (row kernel + combine with the
-    # dense diagonal blocks)
+    # phases: prep (x gathered, exponent, limbs), column (column kernel: Q
+    # codes, the dense diagonal blocks, the row side's B rows), row (row
+    # kernel + combine)
     alg = {
         "prep_x": 8 * n * rhs,                                      # x read once
-        "column": 4 * rw + 16 * comps,                              # Q codes, two scales
-        "row": 4 * lw + 8 * n * rhs + st["dense_bytes"],            # P codes, y written, dense diagonal
+        "column": 4 * rw + 16 * comps + st["dense_bytes"],          # Q codes, two scales, dense diagonal
+        "row": 4 * lw + 8 * n * rhs,                                # P codes, y written
     }
     dom = max(kmean, key=lambda k: kmean[k])
     peak, peak_src = measured_peak()
