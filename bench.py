@@ -396,7 +396,7 @@ def main():
                      "peak_source": peak_src, "algorithmic_bytes": alg[dom],
                      "kernel_ms": {k: round(v, 5) for k, v in kmean.items()},
                      "whole_apply_frac": round(value / world / peak, 4)},
-        "gpu_launches": 5 * K,
+        "gpu_launches": int(st["launches_per_apply"]) * K,
         "clocks": clk.summary(),
         "wall_ms_per_step": round(1e3 * wall / K, 5),
     }

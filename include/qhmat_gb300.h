@@ -74,6 +74,7 @@ typedef struct {
     uint64_t device_bytes;    /* bytes the resident layout occupies on the device */
     uint64_t row_tiles;       /* row-side work units */
     uint64_t flops_per_rhs;   /* 2*(sum rank*(m+n) + sum dense m*n) */
+    uint64_t launches_per_apply; /* kernels one qh_matmul_device call launches */
 } qh_stats;
 
 /* Message of the last failing call made by this thread ("" if none). */

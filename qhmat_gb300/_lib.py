@@ -19,7 +19,8 @@ QH_OK, QH_EINVAL, QH_ERUNTIME, QH_EOVERFLOW, QH_ECUDA = 0, 1, 2, 3, 4
 class QhStats(C.Structure):
     _fields_ = [(name, C.c_uint64) for name in (
         "order", "block_count", "dense_blocks", "lowrank_blocks", "components", "code_bytes",
-        "scale_bytes", "dense_bytes", "model_bytes", "device_bytes", "row_tiles", "flops_per_rhs")]
+        "scale_bytes", "dense_bytes", "model_bytes", "device_bytes", "row_tiles", "flops_per_rhs",
+        "launches_per_apply")]
 
 
 class QhBlockDesc(C.Structure):
