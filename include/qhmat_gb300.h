@@ -152,10 +152,14 @@ QH_API int qh_matmul_device_static(const qh_matrix* m, const double* x, double* 
                                    void* stream, int* status);
 
 /* Drop-in for HMatrix::matmul_cuda: host x (order*rhs doubles), host y.
- * Copies x in through pinned staging, applies, copies y back and
- * synchronises.  Raises the reference's errors: "right-hand-side shape
- * mismatch", "nonfinite right-hand side" (QH_EINVAL), "CUDA launch grid too
- * large" (QH_EOVERFLOW), "no CUDA device is available" (QH_ERUNTIME). */
+ * On a device that reads and writes pageable host memory through the host's
+ * page tables (a coherent host link, as on Grace), the kernels read x and
+ * write y in place; elsewhere, and when x and y overlap, x is copied in
+ * through pinned staging and y copied back.  Synchronises before returning.
+ * Raises the reference's errors: "right-hand-side shape mismatch",
+ * "nonfinite right-hand side" (QH_EINVAL; y is then unspecified), "CUDA
+ * launch grid too large" (QH_EOVERFLOW), "no CUDA device is available"
+ * (QH_ERUNTIME). */
 QH_API int qh_matmul_host(const qh_matrix* m, const double* x, double* y, size_t rhs);
 
 /* FNV-1a-64 of a byte range, the QHMAT001 trailer checksum (offset basis

@@ -436,7 +436,9 @@ __global__ void __launch_bounds__(256) prep_x_kernel(Arena A, Work W, const doub
     const int chunk = blockIdx.x * 8 + warp;
     const int pos = chunk * kChunk + lane;
     const bool valid = chunk < n_chunks && pos < n;
-    const double v = valid ? __ldg(x + (long long)__ldg(A.perm + pos) * rhs + p) : 0.0;
+    // (a plain load: x may be the caller's host memory, read over the
+    // coherent host link)
+    const double v = valid ? x[(long long)__ldg(A.perm + pos) * rhs + p] : 0.0;
     const int e = exp_field(v);
     if (__any_sync(0xFFFFFFFFu, e == 0x7FF) && lane == 0 && status) atomicOr(status, kStatusNonfinite);
     const int em = __reduce_max_sync(0xFFFFFFFFu, e == 0x7FF ? 0 : e);
@@ -1260,6 +1262,9 @@ struct qh_matrix {
     int* d_status = nullptr;
     int* h_status = nullptr;
     cudaStream_t stream = nullptr;
+    // the device reads and writes pageable host memory through the host's
+    // page tables (coherent host link): host-buffer applies need no staging
+    bool host_direct = false;
     ~qh_matrix() {
         int prev = 0;
         cudaGetDevice(&prev);
@@ -1342,6 +1347,12 @@ int upload(Layout&& L, int device, qh_matrix** out) {
     m->L = std::move(L);
     m->device = device;
     cudaDeviceGetAttribute(&m->sms, cudaDevAttrMultiProcessorCount, device);
+    {
+        int pageable = 0, host_tables = 0;
+        cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device);
+        cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device);
+        m->host_direct = pageable == 1 && host_tables == 1;
+    }
     {
         // warp schedules for this device's grids: units longest first, each
         // to the warp with the least predicted time.
@@ -1741,6 +1752,33 @@ int qh_matmul_host(const qh_matrix* m, const double* x, double* y, size_t rhs) {
     }
     const size_t vec = m->L.order * rhs * sizeof(double);
     const size_t need_ws = ws_bytes(m->L, rhs);
+    const auto* xb = reinterpret_cast<const uint8_t*>(x);
+    const auto* yb = reinterpret_cast<const uint8_t*>(y);
+    if (m->host_direct && (xb + vec <= yb || yb + vec <= xb)) {
+        // the kernels read x and write y in the caller's memory directly
+        // (y's pages are written once here first, so that the device never
+        // touches an unpopulated page)
+        if (mm->own_ws_bytes < need_ws) {
+            if (mm->own_ws) cudaFree(mm->own_ws);
+            mm->own_ws = nullptr;
+            mm->own_ws_bytes = 0;
+            e = cudaMalloc(&mm->own_ws, need_ws);
+            if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc");
+            mm->own_ws_bytes = need_ws;
+        }
+        std::memset(y, 0, vec);
+        if ((e = cudaMemsetAsync(mm->d_status, 0, sizeof(int), mm->stream)) != cudaSuccess)
+            return cuda_fail(e, "cudaMemsetAsync");
+        rc = launch(m, x, y, rhs, mm->own_ws, mm->stream, mm->d_status);
+        if (rc) return rc;
+        if ((e = cudaMemcpyAsync(mm->h_status, mm->d_status, sizeof(int), cudaMemcpyDeviceToHost, mm->stream)) !=
+            cudaSuccess)
+            return cuda_fail(e, "cudaMemcpy device-to-host");
+        if ((e = cudaStreamSynchronize(mm->stream)) != cudaSuccess) return cuda_fail(e, "CUDA kernel execution");
+        if (*mm->h_status & kStatusNonfinite) return fail(QH_EINVAL, "nonfinite right-hand side");
+        if (*mm->h_status & kStatusTimeout) return fail(QH_ERUNTIME, "device copy wait timed out");
+        return QH_OK;
+    }
     // one device buffer: workspace | x | y
     const size_t need = align256(need_ws) + 2 * align256(vec);
     if (mm->own_ws_bytes < need) {
