@@ -17,7 +17,9 @@ A step is one apply y = A x.  ``value`` is the packed-byte traffic model
 divided by the device time per step, with x and y resident in HBM; the
 representation (~200 MB) is larger than the 129 MB L2, so no flush is needed
 between steps.  ``e2e`` is the same metric through the host-buffer C-ABI call
-(qh_matmul_host: pinned H2D copy of x, apply, D2H copy of y, all timed).
+(qh_matmul_host: x in from host memory, apply, y out to host memory, all
+timed; on a coherent host link the kernels access the host buffers directly,
+else pinned H2D and D2H copies).
 
 ``--impl reference`` times the reference's CPU HMatrix::matmul on the host
 cores instead: the reference core compiled from its sources (oracle/_ref)
@@ -401,7 +403,7 @@ def main():
         "wall_ms_per_step": round(1e3 * wall / K, 5),
     }
     if rank == 0:
-        # e2e: host buffers through qh_matmul_host (H2D + apply + D2H timed)
+        # e2e: host buffers through qh_matmul_host (x in, apply, y out, timed)
         xh = np.ascontiguousarray(x)
         for _ in range(3):
             h.matmul(xh)
@@ -411,7 +413,10 @@ def main():
         e2e_s = (time.perf_counter() - t0) / args.e2e_steps
         out["e2e"] = {"value": round(model / e2e_s / 1e9, 2), "unit": "GB/s",
                       "h2d_bytes_per_step": int(xh.nbytes), "d2h_bytes_per_step": int(y_host.nbytes),
-                      "ms_per_step": round(1e3 * e2e_s, 4)}
+                      "ms_per_step": round(1e3 * e2e_s, 4),
+                      "transfer": ("x read and y written by the kernels in host memory over the coherent "
+                                   "host link" if st["host_direct"] else
+                                   "pinned staging: H2D copy of x, D2H copy of y")}
         if not args.no_cpu_baseline:
             base, y_cpu = cpu_baseline(data, x, model)
             out["cpu_baseline"] = base

@@ -75,6 +75,7 @@ typedef struct {
     uint64_t row_tiles;       /* row-side work units */
     uint64_t flops_per_rhs;   /* 2*(sum rank*(m+n) + sum dense m*n) */
     uint64_t launches_per_apply; /* kernels one qh_matmul_device call launches */
+    uint64_t host_direct;     /* 1: qh_matmul_host's kernels read x / write y in host memory */
 } qh_stats;
 
 /* Message of the last failing call made by this thread ("" if none). */

@@ -20,7 +20,7 @@ class QhStats(C.Structure):
     _fields_ = [(name, C.c_uint64) for name in (
         "order", "block_count", "dense_blocks", "lowrank_blocks", "components", "code_bytes",
         "scale_bytes", "dense_bytes", "model_bytes", "device_bytes", "row_tiles", "flops_per_rhs",
-        "launches_per_apply")]
+        "launches_per_apply", "host_direct")]
 
 
 class QhBlockDesc(C.Structure):

@@ -1659,6 +1659,7 @@ int qh_matrix_stats(const qh_matrix* m, qh_stats* out) {
     out->row_tiles = uint64_t(L.n_tiles);
     out->flops_per_rhs = L.flops;
     out->launches_per_apply = 3 + (L.n_tasks > 0) + (L.n_units > 0);
+    out->host_direct = m->host_direct ? 1 : 0;
     return QH_OK;
 }
 
