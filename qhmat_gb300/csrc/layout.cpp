@@ -570,19 +570,30 @@ Layout build_layout(const HostMatrix& m) {
                     // 512 bytes of B rows each) filling a row-side stage
                     U.step0 = int32_t(row_steps.size());
                     {
+                        // a step whose k-pairs share one info byte and lie
+                        // wholly inside the k axis is marked uniform (the
+                        // kernel then dispatches once per step)
                         int sc = 0, sb = 0;
+                        bool uni = true;
+                        uint32_t uinfo = 0;
+                        auto flush = [&]() {
+                            row_steps.push_back(uint32_t(sc) | uint32_t(sb / 256) << 8 |
+                                                (uni ? (uinfo << 16) | (1u << 24) : 0u));
+                            sc = 0;
+                            sb = 0;
+                            uni = true;
+                        };
                         for (int32_t kp = h; kp < Kp; kp += T.hsplit) {
                             int cb = 0;
                             for (int mm = 0; mm < kplanes[size_t(kp)]; ++mm) cb += ((knib[size_t(kp)] >> mm) & 1) ? 256 : 512;
-                            if (sc && sb + cb + 512 * (sc + 1) > kRowSlotBytes) {
-                                row_steps.push_back(uint32_t(sc) | uint32_t(sb / 256) << 8);
-                                sc = 0;
-                                sb = 0;
-                            }
+                            if (sc && sb + cb + 512 * (sc + 1) > kRowSlotBytes) flush();
+                            const uint32_t info = kp_info[size_t(kp_off + kp)];
+                            if (sc == 0) uinfo = info;
+                            if (info != uinfo || 32 * (kp + 1) > K) uni = false;
                             ++sc;
                             sb += cb;
                         }
-                        if (sc) row_steps.push_back(uint32_t(sc) | uint32_t(sb / 256) << 8);
+                        if (sc) flush();
                     }
                     U.nsteps = int32_t(row_steps.size()) - U.step0;
                     for (int32_t kp = h; kp < Kp; kp += T.hsplit)

@@ -173,7 +173,9 @@ static_assert(sizeof(TileDense) == 24, "TileDense layout");
 // One warp's unit of row-side work: rows 16q .. 16q + 15 of a tile over the
 // k-pairs kp = h, h + H, ... (nkps of them; B rows from slot0; digit groups
 // from code_off; the tile's k axis has K slots), streamed in nsteps pipeline
-// steps described by row_steps[step0 ..] (k-pairs | code bytes / 256 << 8).
+// steps described by row_steps[step0 ..] (k-pairs | code bytes / 256 << 8 |
+// the k-pairs' common info byte << 16 | 1 << 24 when the step is uniform: one
+// info byte, every k-pair inside the k axis).
 struct RowUnit {
     int32_t tile, q, h, H;
     int32_t nkps, K, slot0, nsteps;

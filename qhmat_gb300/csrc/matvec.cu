@@ -40,6 +40,7 @@
 #include <new>
 #include <numeric>
 #include <queue>
+#include <type_traits>
 #include <string>
 #include <vector>
 
@@ -923,7 +924,7 @@ __global__ void __launch_bounds__(kWarps * 32, QH_ROW_CTAS) row_kernel(Arena A, 
             }
             const uint32_t sw = __shfl_sync(0xFFFFFFFFu, isteps, is - isb);
             const int c = int(sw & 255u);
-            const int cbytes = int(sw >> 8) * 256;
+            const int cbytes = int((sw >> 8) & 255u) * 256;
             const unsigned slot_i = issued % kRowStages;
             uint8_t* slot = slots + slot_i * kRowSlotBytes;
             const unsigned lbytes = unsigned(c * 512);
@@ -1010,11 +1011,40 @@ __global__ void __launch_bounds__(kWarps * 32, QH_ROW_CTAS) row_kernel(Arena A, 
             }
             const uint32_t sw = __shfl_sync(0xFFFFFFFFu, csteps, cs - csb);
             const int c = int(sw & 255u);
-            const int cbytes = int(sw >> 8) * 256;
+            const int cbytes = int((sw >> 8) & 255u) * 256;
             const uint8_t* gp = slot;
             const uint32_t lrow = smem_u32(slot + cbytes) + 16u * unsigned(lane);
+            // a uniform step: one digit pattern, no k slot past the k axis
+            auto run = [&](auto P_, auto NIB_) {
+                constexpr int P = decltype(P_)::value;
+                constexpr bool NIB = decltype(NIB_)::value;
+                const uint32_t hb = kp_hb(int((sw >> 16) & 255u));
+                for (int k = 0; k < c; ++k) {
+                    uint32_t b[4];
+                    limb_frags(lrow + unsigned(k * 512), b);
+                    kp_groups<P, NIB>(D, gp, g, t, b, hb);
+                    gp += P * 512 - (NIB ? 256 : 0);
+                    if (++since == 8) fold_row();
+                }
+            };
+            using I1 = std::integral_constant<int, 1>;
+            using I2 = std::integral_constant<int, 2>;
+            using I3 = std::integral_constant<int, 3>;
+            using I4 = std::integral_constant<int, 4>;
+            if (sw >> 24) {
+                switch ((sw >> 16) & 15u) {
+                    case 4: run(I4{}, std::false_type{}); break;
+                    case 4 | 8: run(I4{}, std::true_type{}); break;
+                    case 3: run(I3{}, std::false_type{}); break;
+                    case 3 | 8: run(I3{}, std::true_type{}); break;
+                    case 2: run(I2{}, std::false_type{}); break;
+                    case 2 | 8: run(I2{}, std::true_type{}); break;
+                    case 1: run(I1{}, std::false_type{}); break;
+                    default: run(I1{}, std::true_type{}); break;
+                }
+            } else
             for (int k = 0; k < c; ++k) {
-                if (ci + k - cib == 32) {
+                if (ci + k - cib >= 32) {
                     cib = ci + k;
                     cinfo = load_info(dc, cib);
                 }

@@ -164,3 +164,23 @@ def test_to_dense_matches_oracle_reconstruct(cuda_device):
     data, _ = golden("ragged300")
     h = HMatrix.from_bytes(data)
     np.testing.assert_array_equal(h.to_dense(), O.OracleMatrix(data).reconstruct())
+
+
+def test_host_apply_in_place_matches(cuda_device):
+    """qh_matmul_host with x and y in one buffer (which takes the pinned
+    staging path even where the kernels can reach host memory directly)
+    gives the same y, bit for bit, as the out-of-place call."""
+    import ctypes as C
+
+    from qhmat_gb300 import _lib
+
+    data, g = golden("cfg1")
+    h = HMatrix.from_bytes(data)
+    x = np.ascontiguousarray(g["x"], dtype=np.float64)
+    y = h.matmul(x, device="cuda")
+    buf = x.copy()
+    lib = _lib.load_library()
+    rc = lib.qh_matmul_host(h._h, buf.ctypes.data_as(C.c_void_p), buf.ctypes.data_as(C.c_void_p), x.shape[1])
+    assert rc == 0
+    assert np.array_equal(buf, y)
+    assert rel_err(buf, g["y"]) <= TOL
