@@ -192,9 +192,12 @@ struct SlotRec {
 };
 
 // Bytes of one column-side shared-memory stage (code groups and x rows of
-// the step's chunks); one row-side stage (code groups and B rows).
-constexpr int kColSlotBytes = 4608;
-constexpr int kRowSlotBytes = 4096;
+// the step's chunks); one row-side stage (code groups and B rows).  Two
+// stages per warp, eight warps per CTA and two CTAs per SM: 6144-byte stages
+// are the largest that fit (measured: larger stages cut the per-step costs;
+// 7168-byte row stages gained nothing more).
+constexpr int kColSlotBytes = 6144;
+constexpr int kRowSlotBytes = 6144;
 // Longest run of chunks one column unit walks.
 constexpr int kMaxPartChunks = 16;
 // Columns of a dense block in one column-side dense unit (one slice).
