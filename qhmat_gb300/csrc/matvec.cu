@@ -19,11 +19,13 @@
 //                      and a width): t_j = sum_i c_ij X_i exactly, then
 //                      u_j = (s^P s^Q) t_j 2^(e-1022-62) in FP64, then u in
 //                      fixed point on each consuming row tile's exponent (a
-//                      layout-time bound) as that tile's B rows (limbs).
+//                      layout-time bound) as that tile's B rows (limbs);
+//                      and warp per dense unit (16 columns of a dense
+//                      diagonal block part, FP64 row sums).
 //   row_kernel         warp per (row tile, 16 rows, k split): sum_j c_ij U_j
 //                      exactly, stored as 128-bit partial sums.
-//   combine_kernel     CTA per row tile: the dense diagonal blocks in FP64,
-//                      plus the partials -> y (one conversion).
+//   combine_kernel     thread per row: dense row sums in column order plus
+//                      the partials -> y (one conversion).
 //
 // The only rounding steps are the fixed-point conversions of x and u (2^-63
 // of the column's largest |x|, of the tile's bound on |u|), the product
@@ -583,17 +585,19 @@ __device__ __forceinline__ void dense_unit(const Arena& A, const Work& W, const 
 }
 
 // Column side.  Warp gw owns the units warp_off[gw] .. warp_off[gw + 1]
-// (assigned longest first at upload, heaviest first per warp); its work
-// is the sequence (unit, rhs column, chunk), streamed through a kColStages-deep
-// pipeline of shared-memory slots filled by bulk copies (the chunks' code
-// groups and the limbs of their x entries), kColStages - 1 steps ahead of their
-// use.  Per chunk the warp runs, for each M-tile and digit plane, two
-// 16x8x16 MMAs (digits x the eight x limbs), plus two with an all-ones A for
-// sum_i X_i (the offset-code correction); the FP32 sums are folded into 64-bit
-// integers every 8 chunks (before any can reach 2^24).  At the unit's end the
-// limbs and planes are combined into exact 128-bit sums t_j = sum_i c_ij X_i,
-// and lane (g, t) converts component 16(t>>1) + 8(t&1) + g to
-// u_j = (s^P s^Q) t_j 2^(xe - 1022 - kFixBits).
+// (assigned longest first at upload by a per-unit cycle model, heaviest first
+// per warp; the first kStagedUnits descriptors are kept in shared memory); its
+// work is the sequence (unit, rhs column, chunk), streamed through a
+// kColStages-deep pipeline of shared-memory slots filled by bulk copies (the
+// chunks' code groups and the limbs of their x entries), kColStages - 1 steps
+// ahead of their use.  Per chunk the warp runs, for each M-tile and digit
+// plane, two 16x8x16 MMAs (digits x the eight x limbs; the top plane's digits
+// signed); the FP32 sums are folded into 64-bit integers every 8 chunks
+// (before any can reach 2^24).  At the unit's end the limbs and planes are
+// combined into exact 128-bit sums t_j = sum_i c_ij X_i (lane j: component j,
+// through shared memory), u_j = (s^P s^Q) t_j 2^(xe - 1022 - kFixBits), and
+// the B rows of u_j on each consuming tile's exponent are written.  Dense
+// units (width 0) are computed in FP64 by dense_unit.
 __global__ void __launch_bounds__(kWarps * 32, QH_COL_CTAS) column_kernel(Arena A, Work W, const int* __restrict__ warp_off,
                                                                 int n_pad, int rhs, int n_split, int n_slots,
                                                                 int n, int n_dslices, int* status) {
