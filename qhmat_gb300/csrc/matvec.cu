@@ -46,6 +46,8 @@
 #include <string>
 #include <vector>
 
+#include <unistd.h>
+
 #include "../../include/qhmat_gb300.h"
 #include "layout.hpp"
 
@@ -1791,8 +1793,8 @@ int qh_matmul_host(const qh_matrix* m, const double* x, double* y, size_t rhs) {
     const auto* yb = reinterpret_cast<const uint8_t*>(y);
     if (m->host_direct && (xb + vec <= yb || yb + vec <= xb)) {
         // the kernels read x and write y in the caller's memory directly
-        // (y's pages are written once here first, so that the device never
-        // touches an unpopulated page)
+        // (each page of y is written once here first, so that the device
+        // never touches an unpopulated page)
         if (mm->own_ws_bytes < need_ws) {
             if (mm->own_ws) cudaFree(mm->own_ws);
             mm->own_ws = nullptr;
@@ -1801,7 +1803,12 @@ int qh_matmul_host(const qh_matrix* m, const double* x, double* y, size_t rhs) {
             if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc");
             mm->own_ws_bytes = need_ws;
         }
-        std::memset(y, 0, vec);
+        {
+            // one write per page makes every page of y present and writable
+            static const uintptr_t page = uintptr_t(sysconf(_SC_PAGESIZE) > 0 ? sysconf(_SC_PAGESIZE) : 4096);
+            const uintptr_t y0 = reinterpret_cast<uintptr_t>(y), y1 = y0 + vec;
+            for (uintptr_t a = y0; a < y1; a = (a & ~(page - 1)) + page) *reinterpret_cast<volatile uint8_t*>(a) = 0;
+        }
         if ((e = cudaMemsetAsync(mm->d_status, 0, sizeof(int), mm->stream)) != cudaSuccess)
             return cuda_fail(e, "cudaMemsetAsync");
         rc = launch(m, x, y, rhs, mm->own_ws, mm->stream, mm->d_status);
