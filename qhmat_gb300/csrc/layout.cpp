@@ -711,6 +711,7 @@ Layout build_layout(const HostMatrix& m) {
     };
     const size_t C = m.width.size();
     S.perm = place(4 * m.order);
+    S.iperm = place(4 * m.order);  // source index -> clustered position
     S.lr = place(sizeof(LowRankDesc) * lr.size());
     S.dd = place(sizeof(DenseDesc) * dd.size());
     S.comp_w = place(C);
@@ -733,7 +734,10 @@ Layout build_layout(const HostMatrix& m) {
 
     L.arena.assign(S.total, 0);
     auto& A = L.arena;
-    for (uint64_t i = 0; i < m.order; ++i) at<int32_t>(A, S.perm)[i] = int32_t(m.permutation[i]);
+    for (uint64_t i = 0; i < m.order; ++i) {
+        at<int32_t>(A, S.perm)[i] = int32_t(m.permutation[i]);
+        at<int32_t>(A, S.iperm)[m.permutation[i]] = int32_t(i);
+    }
     if (!lr.empty()) std::memcpy(at<LowRankDesc>(A, S.lr), lr.data(), sizeof(LowRankDesc) * lr.size());
     if (!dd.empty()) std::memcpy(at<DenseDesc>(A, S.dd), dd.data(), sizeof(DenseDesc) * dd.size());
     for (size_t c = 0; c < C; ++c) {

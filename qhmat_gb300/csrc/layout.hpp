@@ -211,7 +211,7 @@ inline bool top_is_nibble(int w) { return w - 8 * (code_planes(w) - 1) <= 4; }
 
 // Byte offsets of each section inside the device arena.
 struct Sections {
-    size_t perm, lr, dd, comp_w, comp_s, tasks, task_rec, task_dest, qcodes, pcodes, dense, tiles, tdense, units,
+    size_t perm, iperm, lr, dd, comp_w, comp_s, tasks, task_rec, task_dest, qcodes, pcodes, dense, tiles, tdense, units,
         kp_info, slot_rec, row_steps, comp_sl, comp_sr;
     size_t total;
 };

@@ -109,7 +109,8 @@ __device__ __forceinline__ uint4 to_limbs(long long X) {
 }
 
 struct Arena {
-    const int32_t* perm;
+    const int32_t* perm;   // clustered position -> source index
+    const int32_t* iperm;  // source index -> clustered position
     const LowRankDesc* lr;
     const DenseDesc* dd;
     const uint8_t* comp_w;
@@ -429,8 +430,10 @@ __device__ __forceinline__ __int128 ld_i128(const uint4* p) {
                       ((unsigned __int128)v.y << 32) | v.x);
 }
 
-// Block (bx, p) of 8 warps: chunks 8bx .. 8bx+7 of rhs column p.  Clustered
-// FP64 copy of x, the block's largest exponent field, nonfinite flag; the
+// Block (bx, p) of 8 warps: source entries 256bx .. 256bx+255 of rhs column
+// p, read in order (coalesced; x may be the caller's host memory, read over
+// the coherent host link) and stored at their clustered positions as the
+// FP64 copy of x; the block's largest exponent field; nonfinite flag.  The
 // grid also zeroes the apply's counters.
 __global__ void __launch_bounds__(256) prep_x_kernel(Arena A, Work W, const double* __restrict__ x, int n, int rhs,
                                                      int n_chunks, int* zero, int n_zero, int* status) {
@@ -439,15 +442,13 @@ __global__ void __launch_bounds__(256) prep_x_kernel(Arena A, Work W, const doub
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int p = blockIdx.y;
     const int chunk = blockIdx.x * 8 + warp;
-    const int pos = chunk * kChunk + lane;
-    const bool valid = chunk < n_chunks && pos < n;
-    // (a plain load: x may be the caller's host memory, read over the
-    // coherent host link)
-    const double v = valid ? x[(long long)__ldg(A.perm + pos) * rhs + p] : 0.0;
+    const int src = chunk * kChunk + lane;
+    const bool valid = chunk < n_chunks && src < n;
+    const double v = valid ? x[(long long)src * rhs + p] : 0.0;  // (plain load)
     const int e = exp_field(v);
     if (__any_sync(0xFFFFFFFFu, e == 0x7FF) && lane == 0 && status) atomicOr(status, kStatusNonfinite);
     const int em = __reduce_max_sync(0xFFFFFFFFu, e == 0x7FF ? 0 : e);
-    if (valid) W.xc[(long long)p * n + pos] = e == 0x7FF ? 0.0 : v;
+    if (valid) W.xc[(long long)p * n + __ldg(A.iperm + src)] = e == 0x7FF ? 0.0 : v;
     if (lane == 0) s_m[warp] = em;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -1456,6 +1457,7 @@ int upload(Layout&& L, int device, qh_matrix** out) {
     const Sections& S = m->L.sec;
     auto* base = static_cast<const uint8_t*>(m->arena);
     m->A.perm = reinterpret_cast<const int32_t*>(base + S.perm);
+    m->A.iperm = reinterpret_cast<const int32_t*>(base + S.iperm);
     m->A.lr = reinterpret_cast<const LowRankDesc*>(base + S.lr);
     m->A.dd = reinterpret_cast<const DenseDesc*>(base + S.dd);
     m->A.comp_w = base + S.comp_w;
