@@ -31,6 +31,7 @@
 // of the column's largest |x|, of the tile's bound on |u|), the product
 // s^P s^Q, and the final FP64 conversions: the result agrees with the
 // reference's FP64 matmul (src/qhmat/core.cpp:360-390) to ~1e-15 in norm.
+#include <cooperative_groups.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
@@ -435,10 +436,8 @@ __device__ __forceinline__ __int128 ld_i128(const uint4* p) {
 // the coherent host link) and stored at their clustered positions as the
 // FP64 copy of x; the block's largest exponent field; nonfinite flag.  The
 // grid also zeroes the apply's counters.
-__global__ void __launch_bounds__(256) prep_x_kernel(Arena A, Work W, const double* __restrict__ x, int n, int rhs,
-                                                     int n_chunks, int* zero, int n_zero, int* status) {
-    __shared__ int s_m[8];
-    pdl_trigger();
+__device__ __forceinline__ void prep_block(const Arena& A, const Work& W, const double* __restrict__ x, int n,
+                                           int rhs, int n_chunks, int* zero, int n_zero, int* status, int* s_m) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int p = blockIdx.y;
     const int chunk = blockIdx.x * 8 + warp;
@@ -461,25 +460,50 @@ __global__ void __launch_bounds__(256) prep_x_kernel(Arena A, Work W, const doub
     for (long long i = tid; i < n_zero; i += nthr) zero[i] = 0;
 }
 
-// Block (bx, p): the column's exponent from the prep blocks' maxima, then the
-// limbs of X for 256 entries (zero past n).
-__global__ void __launch_bounds__(256) x_limbs_kernel(Work W, int n, int n_pad, int nblk) {
+__global__ void __launch_bounds__(256) prep_x_kernel(Arena A, Work W, const double* __restrict__ x, int n, int rhs,
+                                                     int n_chunks, int* zero, int n_zero, int* status) {
     __shared__ int s_m[8];
     pdl_trigger();
-    pdl_wait();
-    const int p = blockIdx.y, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    prep_block(A, W, x, n, rhs, n_chunks, zero, n_zero, status, s_m);
+}
+
+// Blocks bx = 0, nbx, ... of rhs column p: the column's exponent from the prep
+// blocks' maxima, then the limbs of X for entries bx*256 .. (zero past n).
+__device__ __forceinline__ void limbs_block(const Work& W, int n, int n_pad, int nblk, int p, int bx, int nbx,
+                                            int* s_m) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     int m = 0;
-    for (int i = threadIdx.x; i < nblk; i += blockDim.x) m = max(m, W.xblk[(long long)p * nblk + i]);
+    for (int i = threadIdx.x; i < nblk; i += blockDim.x) m = max(m, __ldcg(W.xblk + (long long)p * nblk + i));
     m = __reduce_max_sync(0xFFFFFFFFu, m);
+    __syncthreads();  // (s_m reused)
     if (lane == 0) s_m[warp] = m;
     __syncthreads();
     int xe = 0;
     for (int i = 0; i < 8; ++i) xe = max(xe, s_m[i]);
-    if (blockIdx.x == 0 && threadIdx.x == 0) W.xe[p] = xe;
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n_pad) return;
-    const long long X = (k < n && xe) ? to_fixed(W.xc[(long long)p * n + k], xe) : 0;
-    W.xq[(long long)p * n_pad + k] = to_limbs(X);
+    if (bx == 0 && threadIdx.x == 0) W.xe[p] = xe;
+    for (int k = bx * blockDim.x + threadIdx.x; k < n_pad; k += nbx * blockDim.x) {
+        const long long X = (k < n && xe) ? to_fixed(__ldcg(W.xc + (long long)p * n + k), xe) : 0;
+        W.xq[(long long)p * n_pad + k] = to_limbs(X);
+    }
+}
+
+__global__ void __launch_bounds__(256) x_limbs_kernel(Work W, int n, int n_pad, int nblk) {
+    __shared__ int s_m[8];
+    pdl_trigger();
+    pdl_wait();
+    limbs_block(W, n, n_pad, nblk, blockIdx.y, blockIdx.x, gridDim.x, s_m);
+}
+
+// prep_x and x_limbs in one cooperative launch (every block resident): the
+// prep work, a grid-wide synchronisation, then the limbs.
+__global__ void __launch_bounds__(256) prep_limbs_kernel(Arena A, Work W, const double* __restrict__ x, int n,
+                                                         int rhs, int n_chunks, int* zero, int n_zero, int* status,
+                                                         int n_pad) {
+    __shared__ int s_m[8];
+    pdl_trigger();
+    prep_block(A, W, x, n, rhs, n_chunks, zero, n_zero, status, s_m);
+    cooperative_groups::this_grid().sync();
+    limbs_block(W, n, n_pad, gridDim.x, blockIdx.y, blockIdx.x, gridDim.x, s_m);
 }
 
 // Bring a line into L1 ahead of its use (no register waits on it).
@@ -491,7 +515,6 @@ __device__ __forceinline__ void cp_async8(void* dst, const void* src) {
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
-// A column unit's descriptor (four 16-byte loads, cached in L1).
 // A column unit's descriptor from four 16-byte words (shared or global).
 __device__ __forceinline__ ColTask load_task(const int4* q) {
     const int4 a = q[0], b = q[1], c = q[2], d = q[3];
@@ -1302,6 +1325,9 @@ struct qh_matrix {
     // the device reads and writes pageable host memory through the host's
     // page tables (coherent host link): host-buffer applies need no staging
     bool host_direct = false;
+    // most blocks of prep_limbs_kernel the device holds at once (0: no
+    // cooperative launch)
+    int prep_coop_max = 0;
     ~qh_matrix() {
         int prev = 0;
         cudaGetDevice(&prev);
@@ -1389,6 +1415,11 @@ int upload(Layout&& L, int device, qh_matrix** out) {
         cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device);
         cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device);
         m->host_direct = pageable == 1 && host_tables == 1;
+        int coop = 0, per_sm = 0;
+        cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device);
+        if (coop && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, prep_limbs_kernel, 256, 0) == cudaSuccess)
+            m->prep_coop_max = per_sm * m->sms;
+        cudaGetLastError();
     }
     {
         // warp schedules for this device's grids: units longest first, each
@@ -1568,11 +1599,28 @@ int launch(const qh_matrix* m, const double* x, double* y, size_t rhs, void* ws,
     };
     const int irhs = int(rhs);
     mark(0);
-    prep_x_kernel<<<dim3(unsigned(P.nblk), unsigned(rhs)), 256, 0, s>>>(
-        m->A, W, x, n, irhs, L.n_chunks, reinterpret_cast<int*>(w + P.zero0), int(P.zero_bytes / 4), status);
     const int n_pad = int(padded_order(L));
-    cudaError_t e = launch_pdl(x_limbs_kernel, dim3(unsigned((n_pad + 255) / 256), unsigned(rhs)), dim3(256), 0, s,
-                               W, n, n_pad, P.nblk);
+    int* zero = reinterpret_cast<int*>(w + P.zero0);
+    const int n_zero = int(P.zero_bytes / 4);
+    cudaError_t e;
+    if (static_cast<long long>(P.nblk) * irhs <= m->prep_coop_max) {
+        // one cooperative launch: prep, a grid-wide synchronisation, limbs
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(unsigned(P.nblk), unsigned(rhs));
+        cfg.blockDim = dim3(256);
+        cfg.stream = s;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeCooperative;
+        attr[0].val.cooperative = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        e = cudaLaunchKernelEx(&cfg, prep_limbs_kernel, m->A, W, x, n, irhs, L.n_chunks, zero, n_zero, status, n_pad);
+    } else {
+        prep_x_kernel<<<dim3(unsigned(P.nblk), unsigned(rhs)), 256, 0, s>>>(m->A, W, x, n, irhs, L.n_chunks, zero,
+                                                                            n_zero, status);
+        e = launch_pdl(x_limbs_kernel, dim3(unsigned((n_pad + 255) / 256), unsigned(rhs)), dim3(256), 0, s, W, n,
+                       n_pad, P.nblk);
+    }
     mark(1);
     if (e == cudaSuccess && L.n_tasks > 0)
         e = launch_pdl(column_kernel, dim3(unsigned(m->col_grid)), dim3(kWarps * 32), size_t(kColPipeSmem), s, m->A,
@@ -1696,7 +1744,8 @@ int qh_matrix_stats(const qh_matrix* m, qh_stats* out) {
     out->device_bytes = L.sec.total;
     out->row_tiles = uint64_t(L.n_tiles);
     out->flops_per_rhs = L.flops;
-    out->launches_per_apply = 3 + (L.n_tasks > 0) + (L.n_units > 0);
+    const WsPlan P1 = ws_plan(L, 1);
+    out->launches_per_apply = (P1.nblk <= m->prep_coop_max ? 2 : 3) + (L.n_tasks > 0) + (L.n_units > 0);
     out->host_direct = m->host_direct ? 1 : 0;
     return QH_OK;
 }

@@ -184,3 +184,20 @@ def test_host_apply_in_place_matches(cuda_device):
     assert rc == 0
     assert np.array_equal(buf, y)
     assert rel_err(buf, g["y"]) <= TOL
+
+
+def test_many_rhs_columns_match_single_column_applies(cuda_device):
+    """200 right-hand sides at n=2048 (more prep blocks than the device holds
+    at once, so prep and limbs run as two launches instead of one cooperative
+    launch): every column equals its own single-column apply bit for bit, and
+    the reference's result within the tolerance."""
+    data, g = golden("cfg1")
+    h = HMatrix.from_bytes(data)
+    m = O.OracleMatrix(data)
+    x = np.random.default_rng(7).standard_normal((h.order, 200))
+    y = h.matmul(x, device="cuda")
+    for p in (0, 1, 57, 199):
+        yp = h.matmul(np.ascontiguousarray(x[:, p]), device="cuda")
+        assert np.array_equal(y[:, p], yp)
+    yr = m.matmul(np.ascontiguousarray(x[:, :4]))
+    assert rel_err(y[:, :4], yr) <= TOL
