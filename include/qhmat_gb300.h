@@ -115,7 +115,9 @@ QH_API size_t qh_workspace_bytes(const qh_matrix* m, size_t rhs);
 /* y = A x on the device.  x, y: device pointers, row-major order x rhs, source
  * order.  workspace: device scratch of at least qh_workspace_bytes(m, rhs)
  * bytes, 256-byte aligned, not shared with a concurrent call; NULL uses a
- * buffer the handle allocates on first use.  stream: a cudaStream_t (NULL =
+ * buffer the handle allocates on first use (shared by all NULL-workspace
+ * calls on the handle, which must therefore not overlap on the GPU; separate
+ * from qh_matmul_host's buffers).  stream: a cudaStream_t (NULL =
  * legacy default stream).  status: optional device int that the call sets to 1
  * when x holds a NaN or infinity (and leaves untouched otherwise); y is then
  * unspecified.  Stream-ordered: returns once the work is enqueued. */

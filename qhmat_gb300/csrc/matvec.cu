@@ -1315,8 +1315,10 @@ struct qh_matrix {
     int col_grid = 0, row_grid = 0;
     // lazily allocated scratch for calls without a workspace, and host staging
     std::mutex mu;
-    void* own_ws = nullptr;
+    void* own_ws = nullptr;  // qh_matmul_host's device buffer
     size_t own_ws_bytes = 0;
+    void* dev_ws = nullptr;  // the workspace of qh_matmul_device calls without one
+    size_t dev_ws_bytes = 0;
     double* pinned = nullptr;
     size_t pinned_bytes = 0;
     int* d_status = nullptr;
@@ -1335,6 +1337,7 @@ struct qh_matrix {
         if (arena) cudaFree(arena);
         if (sched) cudaFree(sched);
         if (own_ws) cudaFree(own_ws);
+        if (dev_ws) cudaFree(dev_ws);
         if (d_status) cudaFree(d_status);
         if (pinned) cudaFreeHost(pinned);
         if (h_status) cudaFreeHost(h_status);
@@ -1774,15 +1777,15 @@ int qh_matmul_device_profiled(const qh_matrix* m, const double* x, double* y, si
     }
     auto* mm = const_cast<qh_matrix*>(m);
     std::lock_guard<std::mutex> lock(mm->mu);
-    if (mm->own_ws_bytes < need) {
-        if (mm->own_ws) cudaFree(mm->own_ws);
-        mm->own_ws = nullptr;
-        mm->own_ws_bytes = 0;
-        cudaError_t e = cudaMalloc(&mm->own_ws, need);
+    if (mm->dev_ws_bytes < need) {
+        if (mm->dev_ws) cudaFree(mm->dev_ws);
+        mm->dev_ws = nullptr;
+        mm->dev_ws_bytes = 0;
+        cudaError_t e = cudaMalloc(&mm->dev_ws, need);
         if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc");
-        mm->own_ws_bytes = need;
+        mm->dev_ws_bytes = need;
     }
-    return launch(m, x, y, rhs, mm->own_ws, static_cast<cudaStream_t>(stream), status, events4);
+    return launch(m, x, y, rhs, mm->dev_ws, static_cast<cudaStream_t>(stream), status, events4);
 }
 
 int qh_matmul_device_static(const qh_matrix* m, const double* x, double* y, size_t rhs, void* stream,
