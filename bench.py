@@ -24,7 +24,13 @@ else pinned H2D and D2H copies).
 ``--impl reference`` times the reference's CPU HMatrix::matmul on the host
 cores instead: the reference core compiled from its sources (oracle/_ref)
 where that build loads, else the bit-identical plain-C restatement
-(oracle/qhmat_oracle.c) with every host thread.
+(oracle/qhmat_oracle.c) with every host thread (and, for comparison, on one
+thread, as the reference runs).  That process never loads the CUDA library.
+Both arms print the same ``config``.
+
+The line also states the result's error against the FP64 dense product A x
+(evaluated from the points, outside the timed region) and samples the SM
+clocks with nvidia-smi over a load window around the timed region.
 """
 
 from __future__ import annotations
@@ -50,7 +56,10 @@ WORKLOADS = {
 }
 
 
-def make_inputs(name: str, workers: int):
+def make_inputs(name: str, workers: int, checksum=None, with_points: bool = False):
+    """(QHMAT001 image, x, construction seconds[, points]) of a workload.
+
+    ``checksum`` computes the image's trailer (default: the library's FNV-1a)."""
     import numpy as np
 
     from qhmat_gb300 import construct
@@ -66,12 +75,17 @@ def make_inputs(name: str, workers: int):
     t0 = time.time()
     img = construct.from_kernel(pts, wl["kernel"], tolerance=wl["tol"], leaf_size=wl["leaf"],
                                 workers=workers)
-    data = construct.to_qhmat_bytes(img)
+    data = construct.to_qhmat_bytes(img, checksum=checksum)
+    if with_points:
+        return data, x, time.time() - t0, pts
     return data, x, time.time() - t0
 
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks and throttle reasons, one sample every 200 ms, read by a
+    background thread.  ``wait_first()`` blocks until the first sample has
+    arrived (nvidia-smi takes a moment to start), so that the load window
+    around the timed region is covered."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -80,32 +94,61 @@ class ClockSampler:
     def __init__(self, index: int):
         self.index = index
         self.proc = None
+        self.lines: list[str] = []
+        self.error = ""
+        self._thread = None
 
     def __enter__(self):
+        import shutil
+        import threading
+
+        exe = shutil.which("nvidia-smi")
+        if exe is None:
+            self.error = "nvidia-smi not found on PATH"
+            return self
         try:
             self.proc = subprocess.Popen(
-                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                [exe, f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
                  "-i", str(self.index), "-lms", "200"],
-                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-        except OSError:
-            self.proc = None
+                stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)
+        except OSError as exc:
+            self.error = f"nvidia-smi failed to start: {exc}"
+            return self
+
+        def reader():
+            for ln in self.proc.stdout:
+                if ln.strip():
+                    self.lines.append(ln.strip())
+
+        self._thread = threading.Thread(target=reader, daemon=True)
+        self._thread.start()
         return self
 
+    def wait_first(self, timeout: float = 10.0) -> bool:
+        t0 = time.time()
+        while self.proc is not None and not self.lines and time.time() - t0 < timeout:
+            if self.proc.poll() is not None:
+                break
+            time.sleep(0.02)
+        return bool(self.lines)
+
     def __exit__(self, *exc):
-        self.lines = []
         if self.proc is not None:
             self.proc.terminate()
             try:
-                out, _ = self.proc.communicate(timeout=5)
+                _, err = self.proc.communicate(timeout=5)
             except subprocess.TimeoutExpired:
                 self.proc.kill()
-                out, _ = self.proc.communicate()
-            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+                _, err = self.proc.communicate()
+            if self._thread is not None:
+                self._thread.join(timeout=5)
+            if not self.lines and err:
+                self.error = "nvidia-smi: " + err.strip().splitlines()[-1][:200]
 
     def summary(self) -> dict:
         sm, mx, reasons = [], [], set()
         names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
-        for ln in getattr(self, "lines", []):
+        for ln in self.lines:
             f = [v.strip() for v in ln.split(",")]
             if len(f) < 9:
                 continue
@@ -118,9 +161,12 @@ class ClockSampler:
                 if v.lower().startswith("active"):
                     reasons.add(name)
         if not sm:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0,
+                    "note": self.error or "no samples"}
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm),
+                "window": "every 200 ms while the GPU ran untimed applies, the timed applies, "
+                          "and untimed applies again (>= 1 s of load around the timed region)"}
 
 
 def measured_peak():
@@ -131,8 +177,14 @@ def measured_peak():
     return 6800.0, "fallback (6.8 TB/s)"
 
 
-def cpu_baseline(data: bytes, x, model_bytes: int, budget_s: float = 10.0) -> dict:
-    """Reference-arm CPU apply on all host cores over a bounded sample."""
+def cpu_baseline(data: bytes, x, model_bytes: int, budget_s: float = 10.0) -> tuple[dict, object]:
+    """The reference's CPU apply on the host cores over a bounded sample.
+
+    The reference core compiled from its sources (oracle/_ref) where that
+    build loads on this machine (it is single-threaded, as written), else the
+    bit-identical C restatement (oracle/qhmat_oracle.c) on every host thread,
+    plus a single-thread run of the same for comparison with the reference's
+    own threading."""
     from oracle import oracle
 
     threads = os.cpu_count() or 1
@@ -146,18 +198,32 @@ def cpu_baseline(data: bytes, x, model_bytes: int, budget_s: float = 10.0) -> di
     if impl is None:
         impl = oracle.OracleMatrix(data)
 
-    def run():
-        return impl.matmul(x) if kind == "reference" else impl.matmul(x, threads=threads)
+    def timed(fn, budget):
+        y = fn()  # warm-up
+        reps, t0 = 0, time.perf_counter()
+        while reps < 3 or (time.perf_counter() - t0 < budget and reps < 10000):
+            fn()
+            reps += 1
+        return y, reps, time.perf_counter() - t0
 
-    y = run()  # warm-up
-    reps, t0 = 0, time.perf_counter()
-    while reps < 3 or (time.perf_counter() - t0 < budget_s and reps < 10000):
-        run()
-        reps += 1
-    dt = time.perf_counter() - t0
-    return {"value": model_bytes * reps / dt / 1e9, "unit": "GB/s", "cores": threads, "kind": kind,
-            "sample": f"{reps} full applies of the bench workload in {dt:.1f} s "
-                      f"({1e3 * dt / reps:.2f} ms each, {threads} thread(s))"}, y
+    if kind == "reference":
+        y, reps, dt = timed(lambda: impl.matmul(x), budget_s)
+    else:
+        y, reps, dt = timed(lambda: impl.matmul(x, threads=threads), budget_s)
+    out = {"value": model_bytes * reps / dt / 1e9, "unit": "GB/s", "cores": threads, "kind": kind,
+           "sample": f"{reps} full applies of the bench workload in {dt:.1f} s "
+                     f"({1e3 * dt / reps:.2f} ms each, {threads} thread(s))",
+           "ms_per_apply": 1e3 * dt / reps}
+    if kind == "port" and threads > 1:
+        _, r1, d1 = timed(lambda: impl.matmul(x, threads=1), min(budget_s, 5.0))
+        out["single_thread"] = {"value": model_bytes * r1 / d1 / 1e9, "unit": "GB/s", "cores": 1,
+                                "ms_per_apply": 1e3 * d1 / r1,
+                                "note": "the same port on one thread (the reference's matmul is "
+                                        "single-threaded)"}
+    if kind == "port":
+        out["why_port"] = ("the reference core is compiled from its own sources where they lie; "
+                           "they are not on this machine, and no copy of them travels with the repo")
+    return out, y
 
 
 def dist_setup():
@@ -186,25 +252,23 @@ def whole_job_gbs(model_bytes: int, world: int, ms_per_step: float) -> float:
 
 
 def run_reference_arm(args):
+    """The reference's CPU apply on the bench workload (rank 0 only).  This
+    process never loads the CUDA library: the image's trailer is computed by
+    the C restatement, and the model bytes are read from the image."""
     world, rank, _ = dist_setup()
     if rank != 0:
         return 0
-    import numpy as np
-
-    data, x, build_s = make_inputs(args.workload, os.cpu_count() or 1)
     from oracle import oracle
 
+    data, x, build_s = make_inputs(args.workload, os.cpu_count() or 1, checksum=oracle.fnv1a64)
     wl = WORKLOADS[args.workload]
-    m = oracle.OracleMatrix(data)
-    import ctypes
-
     model = _model_bytes(data, x)
     base, _ = cpu_baseline(data, x, model, budget_s=min(30.0, 5.0 + 0.02 * args.steps))
     out = {
-        "impl": "reference", "metric": "H-matvec GB/s (% HBM peak)", "value": base["value"], "unit": "GB/s",
+        "impl": "reference", "metric": METRIC, "value": base["value"], "unit": "GB/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": model / (base["value"] * 1e9) * 1e3, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (constructed on the host, seeded)",
+        "vs_baseline": None, "dtype": "f64", "data": DATA_NOTE,
         "config": _config(args.workload, wl, build_s),
         "cpu_baseline": base,
         "e2e": {"value": base["value"], "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -214,7 +278,8 @@ def run_reference_arm(args):
 
 
 def _model_bytes(data: bytes, x) -> int:
-    """Packed-byte model from a QHMAT001 image (no device needed)."""
+    """Packed-byte model from a QHMAT001 image (read by the C restatement; no
+    device needed)."""
     from oracle import oracle
 
     m = oracle.OracleMatrix(data)
@@ -230,13 +295,44 @@ def _model_bytes(data: bytes, x) -> int:
     return codes + scales + dense + 16 * m.order * rhs
 
 
+METRIC = "H-matvec GB/s (% HBM peak)"
+DATA_NOTE = "synthetic (seeded points; matrix constructed on the host)"
+
+
 def _config(name, wl, build_s):
+    """The workload description, identical in both arms."""
     return {"workload": f"{name}: {wl['desc']}", "n": wl["n"], "rhs": wl["rhs"],
             "tolerance": wl["tol"], "tolerance_requested": wl["tol_requested"],
             "tolerance_note": ("requested tolerance infeasible in the reference; tightest feasible of "
                                "the ladder 1e-8/3e-8/1e-7/3e-7/1e-6") if wl["tol"] != wl["tol_requested"] else "",
             "l2": "representation larger than L2 (129 MB); no flush between steps",
             "construction_s": round(build_s, 1)}
+
+
+def dense_oracle_error(pts, kernel: str, x, y, device) -> dict:
+    """||y - A x|| / ||A x|| with A x the FP64 dense product, evaluated on the GPU
+    in row chunks from the points (A itself is never formed); outside any
+    timed region."""
+    import numpy as np
+    import torch
+
+    P = torch.from_numpy(np.ascontiguousarray(pts, dtype=np.float64)).to(device)
+    X = torch.from_numpy(np.ascontiguousarray(x, dtype=np.float64)).to(device)
+    if X.ndim == 1:
+        X = X[:, None]
+    out = torch.empty_like(X)
+    for r0 in range(0, P.shape[0], 1024):
+        r = torch.cdist(P[r0:r0 + 1024], P, compute_mode="donot_use_mm_for_euclid_dist")
+        if kernel == "log":
+            a = -torch.log(r + 1e-3)
+        elif kernel == "inverse":
+            a = 1.0 / (r + 0.4)
+        else:
+            a = torch.exp(-r) / (r + 0.05)
+        out[r0:r0 + 1024] = a @ X
+    ax = out.cpu().numpy().reshape(np.shape(y))
+    return {"rel_err_vs_dense_Ax": float(np.linalg.norm(y - ax) / np.linalg.norm(ax)),
+            "oracle": "FP64 dense A x from the points (GPU, row chunks of 1024; A never stored)"}
 
 
 def main():
@@ -259,7 +355,7 @@ def main():
 
     # Build the matrix (CPU, spawn pool) before the first CUDA call.
     workers = max(1, (os.cpu_count() or 1) // max(1, world))
-    data, x, build_s = make_inputs(args.workload, workers)
+    data, x, build_s, pts = make_inputs(args.workload, workers, with_points=True)
 
     import torch
 
@@ -302,11 +398,20 @@ def main():
         if rc:
             _lib.raise_for(rc)
 
-    def step(i):
+    def step():
         rc = lib.qh_matmul_device(h._h, xd.data_ptr(), yd.data_ptr(), rhs, ws.data_ptr(), need,
                                   stream.cuda_stream, None)
         if rc:
             _lib.raise_for(rc)
+
+    def load_for(seconds):
+        """Untimed applies for about `seconds` (keeps the GPU busy while the
+        clock sampler runs around the timed region)."""
+        t0 = time.perf_counter()
+        while time.perf_counter() - t0 < seconds:
+            for _ in range(50):
+                step()
+            torch.cuda.synchronize()
 
     # Events must exist on the device before their handles are recorded.
     for row in evs:
@@ -316,29 +421,30 @@ def main():
     for i in range(KP):
         step_profiled(i)
     torch.cuda.synchronize()
-    for i in range(W):
-        step(i)
+    for _ in range(W):
+        step()
     torch.cuda.synchronize()
-    if pg:
-        pg.barrier()
     t_start = torch.cuda.Event(enable_timing=True)
     t_end = torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
-        torch.cuda.synchronize()
+        clk.wait_first()
+        load_for(0.6)
         if pg:
             pg.barrier()
+        torch.cuda.synchronize()
         t_start.record(stream)
         wall0 = time.perf_counter()
-        for i in range(W, W + K):
-            step(i)
+        for _ in range(K):
+            step()
         t_end.record(stream)
         torch.cuda.synchronize()
         wall = time.perf_counter() - wall0
         if pg:
             pg.barrier()
+        load_for(0.4)
     total_ms = max_over_ranks(t_start.elapsed_time(t_end), pg, dev)
     ms_step = total_ms / K
-    # per-kernel durations over the timed steps
+    # per-kernel durations (separate pass, events between the phases)
     kern = {"prep_x": [], "column": [], "row": []}
     for i in range(KP):
         e = evs[i]
@@ -346,28 +452,16 @@ def main():
         kern["column"].append(e[1].elapsed_time(e[2]))
         kern["row"].append(e[2].elapsed_time(e[3]))
     kmean = {k: statistics.mean(v) for k, v in kern.items()}
-    # algorithmic bytes per launch of each kernel (packed-byte model split by side)
-    import struct
-
-    # left / right code bytes from the image
-    from oracle import oracle as _o
-
-    om = _o.OracleMatrix(data)
-    lw = rw = 0
-    for b in range(om.block_count):
-        inf = om.block_info(b)
-        if not inf["dense"]:
-            lw += inf["left_words"]
-            rw += inf["right_words"]
+    # algorithmic bytes per launch of each phase (the packed-byte model split
+    # by side): prep (x gathered, exponent, limbs), column (column kernel: Q
+    # codes, two scales, the dense diagonal blocks), row (row kernel +
+    # combine: P codes, y written)
     n = h.order
     comps = st["components"]
-    # phases: prep (x gathered, exponent, limbs), column (column kernel: Q
-    # codes, the dense diagonal blocks, the row side's B rows), row (row
-    # kernel + combine)
     alg = {
-        "prep_x": 8 * n * rhs,                                      # x read once
-        "column": 4 * rw + 16 * comps + st["dense_bytes"],          # Q codes, two scales, dense diagonal
-        "row": 4 * lw + 8 * n * rhs,                                # P codes, y written
+        "prep_x": 8 * n * rhs,
+        "column": st["right_code_bytes"] + 16 * comps + st["dense_bytes"],
+        "row": st["left_code_bytes"] + 8 * n * rhs,
     }
     dom = max(kmean, key=lambda k: kmean[k])
     peak, peak_src = measured_peak()
@@ -381,16 +475,17 @@ def main():
             traffic = None
     value = whole_job_gbs(model, world, ms_step)
 
-    # parity of the timed result against the oracle (same inputs)
     y_gpu = yd.cpu().numpy()
     out = {
-        "metric": "H-matvec GB/s (% HBM peak)", "value": round(value, 2), "unit": "GB/s",
+        "metric": METRIC, "value": round(value, 2), "unit": "GB/s",
         "n_gpus": world, "steps": K, "warmup": W, "ms_per_step": round(ms_step, 5),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64 (int2..int32 codes x 62-bit fixed-point x/u, exact f16 tensor-core digit x limb products; FP64 scales, diagonal)",
-        "data": "synthetic (seeded points; matrix constructed on the host)",
-        "config": dict(_config(args.workload, wl, build_s), parallelism=f"replicas x{world}",
-                       model_bytes=model, components=comps, blocks=st["block_count"]),
+        "dtype": "f64 (int2..int32 codes x 62-bit fixed-point x/u, exact f16 tensor-core digit x limb products; "
+                 "FP64 scales, diagonal)",
+        "data": DATA_NOTE,
+        "config": _config(args.workload, wl, build_s),
+        "workload_stats": {"parallelism": f"replicas x{world}", "model_bytes": model, "components": comps,
+                           "blocks": st["block_count"]},
         "pct_hbm_peak": round(100 * value / world / peak, 1),
         "rhs_per_s": round(rhs * world / (ms_step * 1e-3), 1),
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
@@ -417,6 +512,8 @@ def main():
                       "transfer": ("x read and y written by the kernels in host memory over the coherent "
                                    "host link" if st["host_direct"] else
                                    "pinned staging: H2D copy of x, D2H copy of y")}
+        out["accuracy"] = dense_oracle_error(pts, wl["kernel"], x, y_gpu, dev)
+        out["accuracy"]["reconstruction_bound"] = h.reconstruction_bound
         if not args.no_cpu_baseline:
             base, y_cpu = cpu_baseline(data, x, model)
             out["cpu_baseline"] = base

@@ -51,6 +51,13 @@ extern "C" {
 #define QH_EOVERFLOW 3 /* OverflowError (std::overflow_error) */
 #define QH_ECUDA 4     /* RuntimeError raised from a CUDA runtime failure */
 
+/* Bits the device-side status int of qh_matmul_device / qh_matmul_device_static
+ * may receive (OR-ed in; the call never clears it).  If either is set, y is
+ * unspecified.  qh_matmul_host maps them to QH_EINVAL "nonfinite right-hand
+ * side" and QH_ERUNTIME "device copy wait timed out". */
+#define QH_STATUS_NONFINITE 1 /* x holds a NaN or an infinity */
+#define QH_STATUS_TIMEOUT 2   /* a bounded device wait for a bulk copy gave up */
+
 typedef struct qh_matrix qh_matrix;
 
 /* Mirrors DeviceBlock (src/qhmat/cuda.cu:42-46): one block of the partition in
@@ -76,6 +83,8 @@ typedef struct {
     uint64_t flops_per_rhs;   /* 2*(sum rank*(m+n) + sum dense m*n) */
     uint64_t launches_per_apply; /* kernels one qh_matmul_device call launches */
     uint64_t host_direct;     /* 1: qh_matmul_host's kernels read x / write y in host memory */
+    uint64_t left_code_bytes;  /* 4 * left (row-side, P) code words */
+    uint64_t right_code_bytes; /* 4 * right (column-side, Q) code words */
 } qh_stats;
 
 /* Message of the last failing call made by this thread ("" if none). */
@@ -109,7 +118,9 @@ QH_API int qh_matrix_stats(const qh_matrix* m, qh_stats* out);
  * src/qhmat/core.cpp:467-472). */
 QH_API double qh_matrix_reconstruction_bound(const qh_matrix* m);
 
-/* Device scratch (bytes) one qh_matmul_device call with `rhs` columns needs. */
+/* Device scratch (bytes) one qh_matmul_device call with `rhs` columns needs
+ * (applies with more than 65535 columns run in column chunks of 65535 that
+ * share one chunk's scratch). */
 QH_API size_t qh_workspace_bytes(const qh_matrix* m, size_t rhs);
 
 /* y = A x on the device.  x, y: device pointers, row-major order x rhs, source
@@ -118,9 +129,14 @@ QH_API size_t qh_workspace_bytes(const qh_matrix* m, size_t rhs);
  * buffer the handle allocates on first use (shared by all NULL-workspace
  * calls on the handle, which must therefore not overlap on the GPU; separate
  * from qh_matmul_host's buffers).  stream: a cudaStream_t (NULL =
- * legacy default stream).  status: optional device int that the call sets to 1
- * when x holds a NaN or infinity (and leaves untouched otherwise); y is then
- * unspecified.  Stream-ordered: returns once the work is enqueued. */
+ * legacy default stream).  status: optional device int into which the call
+ * ORs QH_STATUS_NONFINITE (x holds a NaN or infinity) and QH_STATUS_TIMEOUT
+ * (a bounded device wait gave up); it is left untouched otherwise, and y is
+ * unspecified if either bit is set.  Errors before any device work follow the
+ * reference (src/qhmat/cuda.cu:108-112): rhs == 0 -> QH_EINVAL
+ * "right-hand-side shape mismatch", order * rhs > INT_MAX * 256 ->
+ * QH_EOVERFLOW "CUDA launch grid too large".  Stream-ordered: returns once
+ * the work is enqueued. */
 QH_API int qh_matmul_device(const qh_matrix* m, const double* x, double* y, size_t rhs,
                      void* workspace, size_t workspace_bytes, void* stream, int* status);
 
@@ -143,14 +159,17 @@ QH_API int qh_matmul_device_profiled(const qh_matrix* m, const double* x, double
  * __device__ array of QH_STATIC_SCRATCH_BYTES (16 MiB) that every GPU which
  * loads this library holds until the process exits.  The caller still passes
  * x and y (device pointers, row-major order x rhs, source order), the stream
- * and the optional status int, as for qh_matmul_device.  An apply whose
- * scratch (qh_workspace_bytes(m, rhs)) exceeds QH_STATIC_SCRATCH_BYTES is
- * rejected with QH_EINVAL.  The first call on a device looks up the array's
- * device address (cudaGetSymbolAddress) and caches it; make that first call
- * before any stream capture.  All calls share the one array (each call clears
- * the parts that must start at zero), so calls that overlap on the GPU --
- * concurrent streams, or several threads -- race and must be serialised by
- * the caller.  No counterpart in the reference. */
+ * and the optional status int (QH_STATUS_* bits), as for qh_matmul_device.
+ * An apply whose scratch (qh_workspace_bytes(m, rhs)) exceeds
+ * QH_STATIC_SCRATCH_BYTES is rejected with QH_EINVAL.  The first call on a
+ * device looks up the array's device address (cudaGetSymbolAddress) and
+ * caches it for the life of the process; make that first call before any
+ * stream capture.  A cudaDeviceReset of that device invalidates the cached
+ * address: do not call this entry point on a device after resetting it.  All
+ * calls share the one array (each call clears the parts that must start at
+ * zero), so calls that overlap on the GPU -- concurrent streams, or several
+ * threads -- race and must be serialised by the caller.  No counterpart in
+ * the reference. */
 QH_API int qh_matmul_device_static(const qh_matrix* m, const double* x, double* y, size_t rhs,
                                    void* stream, int* status);
 
@@ -190,6 +209,14 @@ QH_API int qh_matrix_reconstruct(const qh_matrix* m, double* out, size_t out_cou
  * (src/qhmat/core.cpp:269-282) semantics of the resident layout for tests. */
 QH_API int qh_debug_decode(const qh_matrix* m, int side, int32_t* out, size_t out_count,
                            size_t* needed);
+
+/* Test aid for the bounded device waits: one warp on `device` waits at most
+ * `polls` (1 .. 2^20) tests on an mbarrier that nothing completes -- no copy
+ * is issued -- and records the timeout in a status int exactly as the apply
+ * kernels do; returns QH_ERUNTIME "device copy wait timed out" when the bit
+ * came back (the expected outcome), QH_OK if the wait unexpectedly succeeded.
+ * No reference counterpart. */
+QH_API int qh_debug_wait_timeout(int device, int polls);
 
 #ifdef __cplusplus
 }

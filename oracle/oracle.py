@@ -59,6 +59,8 @@ def _load():
         lib.qho_block_info.argtypes = [C.c_void_p, C.c_uint64, C.c_void_p]
         lib.qho_block_widths.argtypes = [C.c_void_p, C.c_uint64, C.c_void_p]
         lib.qho_block_codes.argtypes = [C.c_void_p, C.c_uint64, C.c_int, C.c_void_p]
+        lib.qho_fnv1a64.restype = C.c_uint64
+        lib.qho_fnv1a64.argtypes = [C.c_char_p, C.c_uint64]
         lib.qho_bound.restype = C.c_double
         lib.qho_bound.argtypes = [C.c_void_p]
         lib.qho_matmul.restype = C.c_int
@@ -160,6 +162,11 @@ def pack(matrix: np.ndarray, widths) -> tuple[np.ndarray, np.ndarray, np.ndarray
     _load().qho_pack(m.ctypes.data_as(C.c_void_p), rows, _ptr(w), ncomp, _ptr(words),
                      _ptr(offsets), _ptr(scales))
     return words[:nwords], offsets[:ncomp], scales[:ncomp]
+
+
+def fnv1a64(data: bytes) -> int:
+    """QHMAT001 trailer checksum computed by the C restatement."""
+    return int(_load().qho_fnv1a64(data, len(data)))
 
 
 def reference_available() -> bool:

@@ -441,6 +441,14 @@ QHO_EXPORT void qho_block_codes(const qho_matrix* m, uint64_t b, int side, int32
 }
 
 /* core.cpp:467-472 */
+/* FNV-1a-64 of a byte range: the QHMAT001 trailer (io.cpp:18-19, 42).  Lets
+ * the CPU baseline write images without loading the CUDA library. */
+QHO_EXPORT uint64_t qho_fnv1a64(const uint8_t* bytes, uint64_t len) {
+    uint64_t h = FNV_OFFSET;
+    for (uint64_t i = 0; i < len; ++i) h = (h ^ bytes[i]) * FNV_PRIME;
+    return h;
+}
+
 QHO_EXPORT double qho_bound(const qho_matrix* m) {
     double bound = 0.0;
     for (uint64_t b = 0; b < m->block_count; ++b) {

@@ -14,13 +14,15 @@ PKG = Path(__file__).resolve().parent
 LIB_PATH = PKG / "libqhmat_gb300.so"
 
 QH_OK, QH_EINVAL, QH_ERUNTIME, QH_EOVERFLOW, QH_ECUDA = 0, 1, 2, 3, 4
+# bits of the device-side status int (include/qhmat_gb300.h QH_STATUS_*)
+QH_STATUS_NONFINITE, QH_STATUS_TIMEOUT = 1, 2
 
 
 class QhStats(C.Structure):
     _fields_ = [(name, C.c_uint64) for name in (
         "order", "block_count", "dense_blocks", "lowrank_blocks", "components", "code_bytes",
         "scale_bytes", "dense_bytes", "model_bytes", "device_bytes", "row_tiles", "flops_per_rhs",
-        "launches_per_apply", "host_direct")]
+        "launches_per_apply", "host_direct", "left_code_bytes", "right_code_bytes")]
 
 
 class QhBlockDesc(C.Structure):
@@ -75,6 +77,8 @@ def load_library() -> C.CDLL:
     lib.qh_fnv1a64.argtypes = [C.c_char_p, sz]
     lib.qh_debug_decode.restype = i32
     lib.qh_debug_decode.argtypes = [vp, i32, vp, sz, C.POINTER(sz)]
+    lib.qh_debug_wait_timeout.restype = i32
+    lib.qh_debug_wait_timeout.argtypes = [i32, i32]
     lib.qh_matrix_reconstruct.restype = i32
     lib.qh_matrix_reconstruct.argtypes = [vp, vp, sz, i32]
     _lib = lib

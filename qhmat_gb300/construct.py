@@ -392,8 +392,11 @@ def _u64(v) -> bytes:
     return int(v).to_bytes(8, "little")
 
 
-def to_qhmat_bytes(img: Image) -> bytes:
-    """Serialise in QHMAT001 (little-endian, FNV-1a-64 trailer)."""
+def to_qhmat_bytes(img: Image, checksum=None) -> bytes:
+    """Serialise in QHMAT001 (little-endian, FNV-1a-64 trailer).
+
+    ``checksum(body) -> int`` computes the trailer; by default the library's
+    ``qh_fnv1a64``."""
     parts = [b"QHMAT001", _u64(1), _u64(img.order), _u64(len(img.blocks)),
              np.asarray(img.permutation, dtype="<u8").tobytes()]
     for b in img.blocks:
@@ -410,6 +413,10 @@ def to_qhmat_bytes(img: Image) -> bytes:
         parts.append(np.asarray(b.left_words, dtype="<u4").tobytes())
         parts.append(np.asarray(b.right_words, dtype="<u4").tobytes())
     body = b"".join(parts)
-    from ._lib import load_library
+    if checksum is None:
+        from ._lib import load_library
 
-    return body + int(load_library().qh_fnv1a64(body, len(body))).to_bytes(8, "little")
+        def checksum(b):
+            return load_library().qh_fnv1a64(b, len(b))
+
+    return body + int(checksum(body)).to_bytes(8, "little")

@@ -11,6 +11,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <numeric>
@@ -309,10 +310,22 @@ inline void put_digit(uint8_t* row, bool nib, int kb, int e, uint32_t d) {
     }
 }
 
+// Longest run of chunks one column unit walks: kMaxPartChunks, or fewer when
+// the environment variable QHMAT_GB300_PART_CHUNKS (1 .. kMaxPartChunks) asks
+// for it -- a test knob that sends short tasks through the split-task path
+// (partial sums combined by the last part); results are bitwise the same.
+int32_t part_chunks_setting() {
+    const char* v = std::getenv("QHMAT_GB300_PART_CHUNKS");
+    if (!v || !*v) return kMaxPartChunks;
+    const long k = std::strtol(v, nullptr, 10);
+    return int32_t(std::min<long>(kMaxPartChunks, std::max<long>(1, k)));
+}
+
 }  // namespace
 
 Layout build_layout(const HostMatrix& m) {
     Layout L;
+    const int32_t part_chunks = part_chunks_setting();
     L.order = m.order;
     L.bound = m.reconstruction_bound();
     if (m.order >= (1ull << 31)) throw overflow_error("matrix order too large for the device layout");
@@ -428,7 +441,7 @@ Layout build_layout(const HostMatrix& m) {
                 const double bound = l1 * std::fabs(m.left_scale[size_t(c)] * m.right_scale[size_t(c)]);
                 if (bound > 0.0 && std::isfinite(bound)) beta[size_t(c)] = int32_t(std::ilogb(bound)) + 2;
             }
-            const int32_t nparts = (nchunks + kMaxPartChunks - 1) / kMaxPartChunks;
+            const int32_t nparts = (nchunks + part_chunks - 1) / part_chunks;
             const int32_t split_id = nparts > 1 ? n_split++ : -1;
             if (split_id >= 0)
                 for (int32_t l = 0; l < count; ++l) comp_part[size_t(comps[t0 + l].second)] = split_id * 33 + l;
@@ -443,8 +456,8 @@ Layout build_layout(const HostMatrix& m) {
                 T.off = int64_t(base);
                 T.stride = stride;
                 T.comp_idx = comp_idx;
-                T.chunk0 = pt * kMaxPartChunks;
-                T.nchunks = std::min(kMaxPartChunks, nchunks - T.chunk0);
+                T.chunk0 = pt * part_chunks;
+                T.nchunks = std::min(part_chunks, nchunks - T.chunk0);
                 T.part = pt;
                 T.nparts = nparts;
                 T.split_id = split_id;

@@ -172,12 +172,14 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
         : "memory");
     return ok != 0;
 }
-// Bounded wait: gives up (returns false) after kWaitLimit tests (seconds at
-// most) instead of hanging; callers record the failure in the status word and
-// stop.
+// Bounded wait: gives up (returns false) after `limit` tests (kWaitLimit:
+// seconds at most) instead of hanging; callers record the failure in the
+// status word, stop issuing copies, give the copies already issued one more
+// bounded wait each and return (best effort: a copy still outstanding after
+// that wait is abandoned with the block).
 constexpr int kWaitLimit = 1 << 22;
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
-    for (int i = 0; i < kWaitLimit; ++i)
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, int limit = kWaitLimit) {
+    for (int i = 0; i < limit; ++i)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
@@ -220,11 +222,26 @@ constexpr int kStagedUnits = 24;
 constexpr int kRowPipeSmem = kWarps * kRowStages * kRowSlotBytes;
 
 // Status bits written by the kernels (status word of the apply).
-constexpr int kStatusNonfinite = 1;
-constexpr int kStatusTimeout = 2;
+constexpr int kStatusNonfinite = QH_STATUS_NONFINITE;
+constexpr int kStatusTimeout = QH_STATUS_TIMEOUT;
 
 __device__ __forceinline__ void flag_timeout(int* status) {
     if (status) atomicOr(status, kStatusTimeout);
+}
+
+// Test aid for the bounded wait: one warp waits, `polls` tests at most, on an
+// mbarrier that nothing ever completes (no copy is issued, so giving up
+// leaves nothing in flight) and records the timeout in the status word
+// exactly as the streaming kernels do.
+__global__ void wait_timeout_kernel(int polls, int* status) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        mbar_init_fence();
+    }
+    __syncwarp();
+    const bool ok = mbar_wait(&bar, 0, polls);
+    if (!ok && threadIdx.x == 0) flag_timeout(status);
 }
 
 // round(v * 2^k) for a 128-bit integer v, as a double, with integer
@@ -437,13 +454,14 @@ __device__ __forceinline__ __int128 ld_i128(const uint4* p) {
 // FP64 copy of x; the block's largest exponent field; nonfinite flag.  The
 // grid also zeroes the apply's counters.
 __device__ __forceinline__ void prep_block(const Arena& A, const Work& W, const double* __restrict__ x, int n,
-                                           int rhs, int n_chunks, int* zero, int n_zero, int* status, int* s_m) {
+                                           long long ld, int n_chunks, int* zero, int n_zero, int* status,
+                                           int* s_m) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int p = blockIdx.y;
     const int chunk = blockIdx.x * 8 + warp;
     const int src = chunk * kChunk + lane;
     const bool valid = chunk < n_chunks && src < n;
-    const double v = valid ? x[(long long)src * rhs + p] : 0.0;  // (plain load)
+    const double v = valid ? x[(long long)src * ld + p] : 0.0;  // (plain load)
     const int e = exp_field(v);
     if (__any_sync(0xFFFFFFFFu, e == 0x7FF) && lane == 0 && status) atomicOr(status, kStatusNonfinite);
     const int em = __reduce_max_sync(0xFFFFFFFFu, e == 0x7FF ? 0 : e);
@@ -460,11 +478,12 @@ __device__ __forceinline__ void prep_block(const Arena& A, const Work& W, const 
     for (long long i = tid; i < n_zero; i += nthr) zero[i] = 0;
 }
 
-__global__ void __launch_bounds__(256) prep_x_kernel(Arena A, Work W, const double* __restrict__ x, int n, int rhs,
-                                                     int n_chunks, int* zero, int n_zero, int* status) {
+__global__ void __launch_bounds__(256) prep_x_kernel(Arena A, Work W, const double* __restrict__ x, int n,
+                                                     long long ld, int n_chunks, int* zero, int n_zero,
+                                                     int* status) {
     __shared__ int s_m[8];
     pdl_trigger();
-    prep_block(A, W, x, n, rhs, n_chunks, zero, n_zero, status, s_m);
+    prep_block(A, W, x, n, ld, n_chunks, zero, n_zero, status, s_m);
 }
 
 // Blocks bx = 0, nbx, ... of rhs column p: the column's exponent from the prep
@@ -497,11 +516,11 @@ __global__ void __launch_bounds__(256) x_limbs_kernel(Work W, int n, int n_pad, 
 // prep_x and x_limbs in one cooperative launch (every block resident): the
 // prep work, a grid-wide synchronisation, then the limbs.
 __global__ void __launch_bounds__(256) prep_limbs_kernel(Arena A, Work W, const double* __restrict__ x, int n,
-                                                         int rhs, int n_chunks, int* zero, int n_zero, int* status,
-                                                         int n_pad) {
+                                                         long long ld, int n_chunks, int* zero, int n_zero,
+                                                         int* status, int n_pad) {
     __shared__ int s_m[8];
     pdl_trigger();
-    prep_block(A, W, x, n, rhs, n_chunks, zero, n_zero, status, s_m);
+    prep_block(A, W, x, n, ld, n_chunks, zero, n_zero, status, s_m);
     cooperative_groups::this_grid().sync();
     limbs_block(W, n, n_pad, gridDim.x, blockIdx.y, blockIdx.x, gridDim.x, s_m);
 }
@@ -1136,7 +1155,7 @@ __global__ void __launch_bounds__(kWarps * 32, QH_ROW_CTAS) row_kernel(Arena A, 
 // the tile's dense slices (column side) added in column order + the low-rank
 // row sums of the tile's units, converted once.
 __global__ void __launch_bounds__(64) combine_kernel(Arena A, Work W, double* __restrict__ y, int n_tiles,
-                                                    int n_dslices, int rhs) {
+                                                    int n_dslices, long long ld) {
     pdl_trigger();
     const int p = blockIdx.y, tile = blockIdx.x, r = threadIdx.x;
     const RowTile T = A.tiles[tile];
@@ -1153,7 +1172,7 @@ __global__ void __launch_bounds__(64) combine_kernel(Arena A, Work W, double* __
     double d = 0.0;
     for (int i = 0; i < T.nds; ++i) d += __ldcg(W.pdense + ((long long)p * n_dslices + T.ds0 + i) * 64 + r);
     const double lr = (xe && T.c_exp != kNoExp) ? i128_ldexp(R, xe + T.c_exp - 1022 - kFixBits) : 0.0;
-    y[(long long)out * rhs + p] = d + lr;
+    y[(long long)out * ld + p] = d + lr;
 }
 
 // Validation: decode every code from the resident layout through the same
@@ -1529,6 +1548,13 @@ int guarded(F&& f) {
     }
 }
 
+// Right-hand-side columns one chain of launches handles at most (gridDim.y
+// of the prep and combine launches); wider applies run column chunks in
+// turn (every column is computed independently, so the result is the same).
+constexpr size_t kMaxRhsChunk = 65535;
+
+size_t rhs_chunk(size_t rhs) { return std::min(rhs, kMaxRhsChunk); }
+
 struct WsPlan {
     size_t xc, xblk, xe, xq, lsplit, cnt, blimb, plr, pdense, total, zero0, zero_bytes;
     int nblk;
@@ -1562,7 +1588,8 @@ WsPlan ws_plan(const Layout& L, size_t rhs) {
     return w;
 }
 
-size_t ws_bytes(const Layout& L, size_t rhs) { return ws_plan(L, rhs).total; }
+// Workspace of an apply with rhs columns (one column chunk's worth).
+size_t ws_bytes(const Layout& L, size_t rhs) { return ws_plan(L, rhs_chunk(rhs)).total; }
 
 // Launch with programmatic stream serialization (the kernel may start while
 // its predecessor finishes; it waits in-kernel for the predecessor's results).
@@ -1581,8 +1608,10 @@ cudaError_t launch_pdl(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, 
     return cudaLaunchKernelEx(&cfg, k, static_cast<KArgs>(args)...);
 }
 
-int launch(const qh_matrix* m, const double* x, double* y, size_t rhs, void* ws, cudaStream_t s,
-           int* status, void* const* ev = nullptr) {
+// One chain of launches for columns [c0, c0 + rhs) of x and y (leading
+// dimension ld).
+int launch_chunk(const qh_matrix* m, const double* x, double* y, size_t rhs, long long ld, void* ws,
+                 cudaStream_t s, int* status, void* const* ev) {
     const Layout& L = m->L;
     const int n = int(L.order);
     auto* w = static_cast<uint8_t*>(ws);
@@ -1617,9 +1646,9 @@ int launch(const qh_matrix* m, const double* x, double* y, size_t rhs, void* ws,
         attr[0].val.cooperative = 1;
         cfg.attrs = attr;
         cfg.numAttrs = 1;
-        e = cudaLaunchKernelEx(&cfg, prep_limbs_kernel, m->A, W, x, n, irhs, L.n_chunks, zero, n_zero, status, n_pad);
+        e = cudaLaunchKernelEx(&cfg, prep_limbs_kernel, m->A, W, x, n, ld, L.n_chunks, zero, n_zero, status, n_pad);
     } else {
-        prep_x_kernel<<<dim3(unsigned(P.nblk), unsigned(rhs)), 256, 0, s>>>(m->A, W, x, n, irhs, L.n_chunks, zero,
+        prep_x_kernel<<<dim3(unsigned(P.nblk), unsigned(rhs)), 256, 0, s>>>(m->A, W, x, n, ld, L.n_chunks, zero,
                                                                             n_zero, status);
         e = launch_pdl(x_limbs_kernel, dim3(unsigned((n_pad + 255) / 256), unsigned(rhs)), dim3(256), 0, s, W, n,
                        n_pad, P.nblk);
@@ -1635,7 +1664,7 @@ int launch(const qh_matrix* m, const double* x, double* y, size_t rhs, void* ws,
                        status);
     if (e == cudaSuccess)
         e = launch_pdl(combine_kernel, dim3(unsigned(L.n_tiles), unsigned(rhs)), dim3(64), 0, s, m->A, W, y,
-                       L.n_tiles, L.n_dslices, irhs);
+                       L.n_tiles, L.n_dslices, ld);
     if (e != cudaSuccess) return cuda_fail(e, "CUDA kernel launch");
     mark(3);
     e = cudaGetLastError();
@@ -1643,10 +1672,25 @@ int launch(const qh_matrix* m, const double* x, double* y, size_t rhs, void* ws,
     return QH_OK;
 }
 
+// The apply: column chunks of at most kMaxRhsChunk, one chain each, in stream
+// order on the same workspace (sized for one chunk).  Events (profiling) are
+// recorded around the first chunk's kernels.
+int launch(const qh_matrix* m, const double* x, double* y, size_t rhs, void* ws, cudaStream_t s,
+           int* status, void* const* ev = nullptr) {
+    for (size_t c0 = 0; c0 < rhs; c0 += kMaxRhsChunk) {
+        const int rc = launch_chunk(m, x + c0, y + c0, std::min(kMaxRhsChunk, rhs - c0), (long long)rhs, ws, s,
+                                    status, c0 == 0 ? ev : nullptr);
+        if (rc) return rc;
+    }
+    return QH_OK;
+}
+
+// The reference's checks (src/qhmat/cuda.cu:108-112): a zero or
+// overflowing column count is a shape mismatch; more than INT_MAX * 256
+// entries is "CUDA launch grid too large".
 int check_rhs(const qh_matrix* m, size_t rhs) {
-    if (rhs == 0 || rhs > SIZE_MAX / m->L.order / 8) return fail(QH_EINVAL, "right-hand-side shape mismatch");
-    if (rhs > size_t(INT32_MAX) || m->L.order * rhs > (size_t(1) << 40))
-        return fail(QH_EOVERFLOW, "CUDA launch grid too large");
+    if (rhs == 0 || rhs > SIZE_MAX / m->L.order) return fail(QH_EINVAL, "right-hand-side shape mismatch");
+    if (m->L.order * rhs > size_t(INT32_MAX) * 256) return fail(QH_EOVERFLOW, "CUDA launch grid too large");
     return QH_OK;
 }
 
@@ -1750,6 +1794,8 @@ int qh_matrix_stats(const qh_matrix* m, qh_stats* out) {
     const WsPlan P1 = ws_plan(L, 1);
     out->launches_per_apply = (P1.nblk <= m->prep_coop_max ? 2 : 3) + (L.n_tasks > 0) + (L.n_units > 0);
     out->host_direct = m->host_direct ? 1 : 0;
+    out->left_code_bytes = L.left_code_bytes;
+    out->right_code_bytes = L.right_code_bytes;
     return QH_OK;
 }
 
@@ -1800,23 +1846,31 @@ int qh_matmul_device_static(const qh_matrix* m, const double* x, double* y, size
                                    " bytes of scratch, more than the fixed " +
                                    std::to_string(size_t(QH_STATIC_SCRATCH_BYTES)) +
                                    " (QH_STATIC_SCRATCH_BYTES); use qh_matmul_device with a workspace");
-    DeviceGuard g(m->device);
     // Device address of the array, looked up once per device with that device
-    // current (the first call on a device does this set-up).
+    // current (the first call on a device does this set-up; a table entry per
+    // device the process sees).
     static std::mutex mu;
-    static void* addr[64] = {nullptr};
-    if (m->device < 0 || m->device >= 64) return fail(QH_EINVAL, "invalid CUDA device ordinal");
+    static std::vector<void*> addr;
     void* ptr = nullptr;
     {
         std::lock_guard<std::mutex> lock(mu);
-        if (!addr[m->device]) {
+        if (addr.empty()) {
+            int count = 0;
+            cudaError_t e = cudaGetDeviceCount(&count);
+            if (e != cudaSuccess) return cuda_fail(e, "cudaGetDeviceCount");
+            addr.assign(size_t(std::max(count, 0)), nullptr);
+        }
+        if (m->device < 0 || size_t(m->device) >= addr.size()) return fail(QH_EINVAL, "invalid CUDA device ordinal");
+        DeviceGuard g(m->device);
+        if (!addr[size_t(m->device)]) {
             void* p = nullptr;
             cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
             if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress");
-            addr[m->device] = p;
+            addr[size_t(m->device)] = p;
         }
-        ptr = addr[m->device];
+        ptr = addr[size_t(m->device)];
     }
+    DeviceGuard g(m->device);
     return launch(m, x, y, rhs, ptr, static_cast<cudaStream_t>(stream), status);
 }
 
@@ -1912,6 +1966,27 @@ int qh_matmul_host(const qh_matrix* m, const double* x, double* y, size_t rhs) {
     if (*mm->h_status & kStatusNonfinite) return fail(QH_EINVAL, "nonfinite right-hand side");
     if (*mm->h_status & kStatusTimeout) return fail(QH_ERUNTIME, "device copy wait timed out");
     std::memcpy(y, mm->pinned, vec);
+    return QH_OK;
+}
+
+int qh_debug_wait_timeout(int device, int polls) {
+    if (polls < 1 || polls > (1 << 20)) return fail(QH_EINVAL, "polls must be in [1, 2^20]");
+    int rc = check_device(device);
+    if (rc) return rc;
+    DeviceGuard g(device);
+    int* d = nullptr;
+    cudaError_t e = cudaMalloc(&d, sizeof(int));
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc");
+    int h = 0;
+    e = cudaMemset(d, 0, sizeof(int));
+    if (e == cudaSuccess) {
+        wait_timeout_kernel<<<1, 32>>>(polls, d);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(&h, d, sizeof(int), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return cuda_fail(e, "debug wait");
+    if (h & kStatusTimeout) return fail(QH_ERUNTIME, "device copy wait timed out");
     return QH_OK;
 }
 

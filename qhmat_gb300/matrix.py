@@ -21,7 +21,7 @@ from pathlib import Path
 
 import numpy as np
 
-from ._lib import QhBlockDesc, QhStats, load_library, raise_for
+from ._lib import QH_STATUS_NONFINITE, QH_STATUS_TIMEOUT, QhBlockDesc, QhStats, load_library, raise_for
 
 
 def _torch():
@@ -182,8 +182,12 @@ class HMatrix:
         raise_for(self._lib.qh_matmul_device(self._h, x.data_ptr(), y.data_ptr(), rhs,
                                              workspace.data_ptr(), need, s.cuda_stream,
                                              status.data_ptr()))
-        if check and int(status.item()):
-            raise ValueError("nonfinite right-hand side")
+        if check:
+            st = int(status.item())
+            if st & QH_STATUS_NONFINITE:
+                raise ValueError("nonfinite right-hand side")
+            if st & QH_STATUS_TIMEOUT:
+                raise RuntimeError("device copy wait timed out")
         return y
 
     def __matmul__(self, x):

@@ -34,3 +34,17 @@ def test_layout_round_trip(checker, name):
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
     assert r.stdout.startswith("OK")
+
+
+@pytest.mark.parametrize("name", ["ragged300", "cfg1", "orth17_b12"])
+def test_layout_round_trip_with_split_tasks(checker, name):
+    """The same checks with every column task longer than one chunk split into
+    one-chunk parts (QHMAT_GB300_PART_CHUNKS=1), the layout the split-task
+    path of the column kernel reads."""
+    import os
+
+    env = dict(os.environ, QHMAT_GB300_PART_CHUNKS="1")
+    r = subprocess.run([str(checker), str(ROOT / "tests" / "golden" / f"{name}.qhmat")],
+                       capture_output=True, text=True, env=env)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert r.stdout.startswith("OK")

@@ -201,3 +201,107 @@ def test_many_rhs_columns_match_single_column_applies(cuda_device):
         assert np.array_equal(y[:, p], yp)
     yr = m.matmul(np.ascontiguousarray(x[:, :4]))
     assert rel_err(y[:, :4], yr) <= TOL
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_split_task_path_is_bitwise_equal(cuda_device, name, monkeypatch):
+    """Every column task cut into one-chunk parts (QHMAT_GB300_PART_CHUNKS=1),
+    so that every fixture with a task of two or more chunks runs the split
+    path (64-bit atomic partial sums, fence, last-finisher counter): the
+    integer sums are exact, so y equals the default layout's bit for bit."""
+    data, g = golden(name)
+    y_default = HMatrix.from_bytes(data).matmul(g["x"])
+    monkeypatch.setenv("QHMAT_GB300_PART_CHUNKS", "1")
+    h = HMatrix.from_bytes(data)
+    y1 = h.matmul(g["x"])
+    y2 = h.matmul(g["x"])
+    assert np.array_equal(y1, y_default)
+    assert np.array_equal(y1, y2)
+    assert rel_err(y1, g["y"]) <= TOL
+
+
+def test_wait_timeout_sets_status(cuda_device):
+    """The bounded device wait gives up and reports QH_STATUS_TIMEOUT, which the
+    host maps to QH_ERUNTIME; the context stays usable afterwards."""
+    from qhmat_gb300 import _lib
+
+    lib = _lib.load_library()
+    rc = lib.qh_debug_wait_timeout(cuda_device, 64)
+    assert rc == _lib.QH_ERUNTIME
+    assert "device copy wait timed out" in lib.qh_last_error().decode()
+    data, g = golden("cfg1")
+    assert rel_err(HMatrix.from_bytes(data).matmul(g["x"]), g["y"]) <= TOL
+
+
+def test_nonfinite_tensor_path_status(cuda_device):
+    """A NaN or infinity in a device x sets QH_STATUS_NONFINITE in the status
+    int (tensor path: ValueError; raw C ABI: the bit)."""
+    import torch
+
+    from qhmat_gb300 import _lib
+
+    data, g = golden("cfg1")
+    h = HMatrix.from_bytes(data)
+    x = torch.from_numpy(g["x"].copy()).cuda()
+    x[17, 2] = float("nan")
+    with pytest.raises(ValueError, match="nonfinite right-hand side"):
+        h.matmul(x)
+    x[17, 2] = float("-inf")
+    lib = _lib.load_library()
+    y = torch.empty_like(x)
+    need = h.workspace_bytes(4)
+    ws = torch.empty(need, dtype=torch.uint8, device=x.device)
+    status = torch.zeros(1, dtype=torch.int32, device=x.device)
+    _lib.raise_for(lib.qh_matmul_device(h._h, x.data_ptr(), y.data_ptr(), 4, ws.data_ptr(), need,
+                                        torch.cuda.current_stream().cuda_stream, status.data_ptr()))
+    assert int(status.item()) == _lib.QH_STATUS_NONFINITE
+    x[17, 2] = 0.5
+    assert rel_err(h.matmul(x).cpu().numpy(), O.OracleMatrix(data).matmul(x.cpu().numpy())) <= TOL
+
+
+def test_more_than_65535_columns(cuda_device):
+    """An apply with 65539 right-hand sides (more than one launch grid's
+    gridDim.y) runs in column chunks: every column equals its own apply bit for
+    bit and the oracle within the tolerance (the reference accepts any rhs with
+    order * rhs <= INT_MAX * 256, src/qhmat/cuda.cu:111-112)."""
+    data, g = golden("cuda10")
+    h = HMatrix.from_bytes(data)
+    rhs = 65539
+    x = np.random.default_rng(5).standard_normal((h.order, rhs))
+    y = h.matmul(x)
+    for p in (0, 65534, 65535, 65538):
+        assert np.array_equal(y[:, p], h.matmul(np.ascontiguousarray(x[:, p])))
+    assert rel_err(y, O.OracleMatrix(data).matmul(x)) <= TOL
+
+
+def test_rhs_limits_match_reference(cuda_device):
+    """rhs = 0 is a shape mismatch and order * rhs > INT_MAX * 256 is "CUDA launch
+    grid too large", both raised before any device work
+    (src/qhmat/cuda.cu:108-112)."""
+    import ctypes as C
+
+    from qhmat_gb300 import _lib
+
+    data, _ = golden("cuda10")
+    h = HMatrix.from_bytes(data)
+    lib = _lib.load_library()
+    dummy = np.zeros(4)
+    p = dummy.ctypes.data_as(C.c_void_p)
+    assert lib.qh_matmul_host(h._h, p, p, 0) == _lib.QH_EINVAL
+    assert "right-hand-side shape mismatch" in lib.qh_last_error().decode()
+    too_many = (2**31 - 1) * 256 // h.order + 1
+    assert lib.qh_matmul_host(h._h, p, p, too_many) == _lib.QH_EOVERFLOW
+    assert "CUDA launch grid too large" in lib.qh_last_error().decode()
+    assert lib.qh_matmul_device(h._h, p, p, too_many, None, 0, None, None) == _lib.QH_EOVERFLOW
+
+
+def test_cpu_device_is_rejected(cuda_device):
+    """The reference's matmul defaults to device="cpu" (python/qhmat/matrix.py:
+    295-303); this library applies on the GPU only and says so instead of
+    falling back to a CPU loop."""
+    data, g = golden("cuda10")
+    h = HMatrix.from_bytes(data)
+    with pytest.raises(ValueError, match="GPU only"):
+        h.matmul(g["x"], device="cpu")
+    with pytest.raises(RuntimeError, match="GPU only"):
+        NativeHMatrix.from_bytes(data).matmul(g["x"], False)

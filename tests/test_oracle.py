@@ -10,7 +10,7 @@ itself on fresh inputs.
 import numpy as np
 import pytest
 
-from conftest import GOLDEN_CASES, golden
+from conftest import GOLDEN_CASES, ROOT, golden
 from oracle import oracle as O
 
 
@@ -158,3 +158,32 @@ def test_oracle_rejects_nonfinite_rhs():
     x[3, 1] = np.nan
     with pytest.raises(ValueError, match="nonfinite"):
         m.matmul(x)
+
+
+def test_oracle_checksum_matches_trailer():
+    """The C restatement's FNV-1a-64 reproduces every fixture's trailer (the
+    CPU baseline writes images with it, without loading the CUDA library)."""
+    for name in ("tiny2", "cfg1", "ragged300"):
+        data = (ROOT / "tests" / "golden" / f"{name}.qhmat").read_bytes()
+        assert O.fnv1a64(data[:-8]) == int.from_bytes(data[-8:], "little")
+
+
+def test_reference_arm_never_loads_the_cuda_library():
+    """bench.py --impl reference on the n=2048 workload: one JSON line with the
+    reference arm's fields and the same config keys as the GPU arm, and the
+    process maps no libqhmat_gb300.so."""
+    import json
+    import subprocess
+    import sys
+
+    code = ("import sys, bench; sys.argv = ['bench.py', '--impl', 'reference', '--workload', 'cfg1', "
+            "'--steps', '3', '--warmup', '3']; bench.main(); "
+            "print('MAPS', open('/proc/self/maps').read().count('libqhmat_gb300'))")
+    r = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    lines = r.stdout.strip().splitlines()
+    assert lines[-1] == "MAPS 0"
+    out = json.loads(lines[-2])
+    assert out["impl"] == "reference" and out["e2e"]["h2d_bytes_per_step"] == 0
+    assert set(out["config"]) == {"workload", "n", "rhs", "tolerance", "tolerance_requested",
+                                  "tolerance_note", "l2", "construction_s"}
