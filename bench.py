@@ -53,7 +53,11 @@ WORKLOADS = {
                       "widths 4/8/12/16/24/32, single RHS"),
     "cfg1": dict(n=2048, dim=1, seed=0, kernel="inverse", leaf=32, tol_requested=1e-6, tol=1e-6, rhs=4,
                  desc="plain CPU-runnable: n=2048 linspace, 1/(r+0.4), leaf 32, RHS 2048x4 seed 0"),
+    "cfg3": dict(n=32768, dim=3, seed=2, kernel="yukawa", leaf=64, tol_requested=1e-6, tol=1e-6, rhs=64,
+                 desc="precision form: n=32768 uniform unit cube (seed 2), exp(-r)/(r+0.05), leaf 64, "
+                      "widths 4/8/12/16/24/32, X 32768x64 N(0,1)"),
 }
+PRECISION_WORKLOADS = {"cfg3"}
 
 
 def make_inputs(name: str, workers: int, checksum=None, with_points: bool = False):
@@ -305,7 +309,7 @@ def _config(name, wl, build_s):
             "tolerance": wl["tol"], "tolerance_requested": wl["tol_requested"],
             "tolerance_note": ("requested tolerance infeasible in the reference; tightest feasible of "
                                "the ladder 1e-8/3e-8/1e-7/3e-7/1e-6") if wl["tol"] != wl["tol_requested"] else "",
-            "l2": "representation larger than L2 (129 MB); no flush between steps",
+            "l2": "representation larger than L2 (129 MB; 1.3 GB for the precision workload); no flush between steps",
             "construction_s": round(build_s, 1)}
 
 
@@ -335,6 +339,205 @@ def dense_oracle_error(pts, kernel: str, x, y, device) -> dict:
             "oracle": "FP64 dense A x from the points (GPU, row chunks of 1024; A never stored)"}
 
 
+def run_precision(args):
+    """The multi-right-hand-side precision form on its workload (X 32768 x 64):
+    RHS/s of the tcgen05 apply (device buffers, CUDA events), beside the plain
+    FP64 form on the same X, the error of both against the dense product, the
+    gate between them, and the tensor / HBM rooflines of the dominant kernel."""
+    import ctypes as C
+
+    import numpy as np
+
+    world, rank, local = dist_setup()
+    workers = max(1, (os.cpu_count() or 1) // max(1, world))
+    data, x, build_s, pts = make_inputs(args.workload, workers, with_points=True)
+
+    import torch
+
+    import qhmat_gb300
+    from qhmat_gb300 import _lib, precision_gate
+
+    torch.cuda.set_device(local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        pg = dist
+    lib = _lib.load_library()
+    wl = WORKLOADS[args.workload]
+    rhs = wl["rhs"]
+    h = qhmat_gb300.HMatrix.from_bytes(data, device=local, precision=True)
+    pf = h._pf
+    pst = pf.stats
+    dev = torch.device("cuda", local)
+    xd = torch.from_numpy(np.ascontiguousarray(x)).to(dev)
+    yd = torch.empty_like(xd)
+    need = pf.workspace_bytes(rhs)
+    ws = torch.empty(need, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        rc = lib.qh_pmatmul_device(pf._h, xd.data_ptr(), yd.data_ptr(), rhs, ws.data_ptr(), need,
+                                   stream.cuda_stream, None)
+        if rc:
+            _lib.raise_for(rc)
+
+    # per-kernel breakdown (separate pass, events between the launches)
+    KP = min(args.steps, 20)
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(5)] for _ in range(KP)]
+    for row in evs:
+        for e in row:
+            e.record(stream)
+    torch.cuda.synchronize()
+    for i in range(KP):
+        arr = (C.c_void_p * 5)(*[e.cuda_event for e in evs[i]])
+        _lib.raise_for(lib.qh_pmatmul_device_profiled(pf._h, xd.data_ptr(), yd.data_ptr(), rhs, ws.data_ptr(), need,
+                                                      stream.cuda_stream, None, arr))
+    torch.cuda.synchronize()
+    names = ["prep", "column", "row", "combine"]
+    kmean = {k: statistics.mean(evs[i][j].elapsed_time(evs[i][j + 1]) for i in range(KP))
+             for j, k in enumerate(names)}
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    K = args.steps
+    t0e, t1e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        clk.wait_first()
+        t_load = time.perf_counter()
+        while time.perf_counter() - t_load < 0.6:
+            step()
+            torch.cuda.synchronize()
+        if pg:
+            pg.barrier()
+        torch.cuda.synchronize()
+        t0e.record(stream)
+        for _ in range(K):
+            step()
+        t1e.record(stream)
+        torch.cuda.synchronize()
+        if pg:
+            pg.barrier()
+        t_load = time.perf_counter()
+        while time.perf_counter() - t_load < 0.4:
+            step()
+            torch.cuda.synchronize()
+    ms_step = max_over_ranks(t0e.elapsed_time(t1e), pg, dev) / K
+    y_pf = yd.cpu().numpy()
+
+    # the plain FP64 form on the same X (device buffers; one chain per apply)
+    nplain = 3
+    ws_plain = torch.empty(h.workspace_bytes(rhs), dtype=torch.uint8, device=dev)
+    yp = torch.empty_like(xd)
+
+    def plain_step():
+        _lib.raise_for(lib.qh_matmul_device(h._h, xd.data_ptr(), yp.data_ptr(), rhs, ws_plain.data_ptr(),
+                                            ws_plain.numel(), stream.cuda_stream, None))
+
+    plain_step()
+    torch.cuda.synchronize()
+    p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    p0.record(stream)
+    for _ in range(nplain):
+        plain_step()
+    p1.record(stream)
+    torch.cuda.synchronize()
+    ms_plain = p0.elapsed_time(p1) / nplain
+    y_plain = yp.cpu().numpy()
+
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    tc_peak = float(peaks.get("bf16_tflops", 1900.0))
+    N = 3 * min(rhs, 64)
+    n = h.order
+    nslot = pst["row_slots"]
+    pu = (min(rhs, 64) + 15) // 16 * 16
+    # per kernel: MMA flops issued (f16, N = 3p limb columns) and the bytes it
+    # must move (digit planes / limb tiles, u per slot, x limbs, partials)
+    kflops = {"column": 2.0 * pst["mma_col_elements"] * N, "row": 2.0 * pst["mma_row_elements"] * N}
+    kbytes = {"column": pst["stored_q_bytes"] + 4 * nslot * pu + 2 * N * n,
+              "row": pst["stored_p_bytes"] + pst["stored_dense_bytes"] + 4 * nslot * pu + 8 * n * pu}
+    dom = max(("column", "row"), key=lambda k: kmean[k])
+    tfrac = kflops[dom] / (kmean[dom] * 1e-3) / 1e12 / tc_peak
+    hfrac = kbytes[dom] / (kmean[dom] * 1e-3) / 1e9 / hbm_peak
+    bound = "tensor" if tfrac >= hfrac else "hbm"
+    achieved = (kflops[dom] / (kmean[dom] * 1e-3) / 1e12) if bound == "tensor" else \
+        (kbytes[dom] / (kmean[dom] * 1e-3) / 1e9)
+    model_bytes = h.model_bytes(rhs)
+    model_flops = rhs * h.stats["flops_per_rhs"]
+    value = rhs * world / (ms_step * 1e-3)
+    out = {
+        "metric": "H-matvec RHS/s (precision form, X 32768x64)", "value": round(value, 1), "unit": "RHS/s",
+        "n_gpus": world, "steps": K, "warmup": args.warmup, "ms_per_step": round(ms_step, 5),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f16 digit planes x f16 hi/mid/lo limbs of x and u, f32 accumulate (tcgen05, TMEM); "
+                 "f64 scales, dense-limb sums and y",
+        "data": DATA_NOTE, "config": _config(args.workload, wl, build_s),
+        "roofline": {"bound": bound, "kernel": dom, "achieved": round(achieved, 1),
+                     "peak": tc_peak if bound == "tensor" else hbm_peak,
+                     "unit": "TFLOP/s" if bound == "tensor" else "GB/s",
+                     "frac": round(max(tfrac, hfrac), 4), "traffic": None,
+                     "tensor_frac": round(tfrac, 4), "hbm_frac": round(hfrac, 4),
+                     "kernel_ms": {k: round(v, 5) for k, v in kmean.items()},
+                     "mma_flops": kflops, "moved_bytes": kbytes,
+                     "peak_source": "MEASURED_PEAKS.json (bf16_tflops burst; f16 runs at the bf16 rate; hbm_gbs)"},
+        "model": {"packed_bytes": model_bytes, "flops": model_flops,
+                  "packed_gbs": round(model_bytes / (ms_step * 1e-3) / 1e9, 1)},
+        "plain_form": {"ms_per_apply": round(ms_plain, 4), "rhs_per_s": round(rhs / (ms_plain * 1e-3), 1),
+                       "speedup_of_precision_form": round(ms_plain / ms_step, 2)},
+        "gpu_launches": int(pst["launches_per_pass"]) * ((rhs + 63) // 64) * K,
+        "clocks": clk.summary(),
+        "stats": pst,
+    }
+    if rank == 0:
+        gate = precision_gate(y_pf, y_plain, x, h.reconstruction_bound)
+        acc_pf = dense_oracle_error(pts, wl["kernel"], x, y_pf, dev)
+        acc_plain = dense_oracle_error(pts, wl["kernel"], x, y_plain, dev)
+        out["accuracy"] = {
+            "precision_rel_err_vs_dense_Ax": acc_pf["rel_err_vs_dense_Ax"],
+            "plain_rel_err_vs_dense_Ax": acc_plain["rel_err_vs_dense_Ax"],
+            "gate": "per column max|y_pf - y_plain| <= 0.01 * reconstruction_bound * ||x||_1",
+            "gate_worst_ratio": gate["worst_ratio"], "gate_passes": gate["passes"],
+            "max_abs_dev_vs_plain": gate["max_abs_dev"], "rel_dev_vs_plain": gate["rel_err"],
+            "raw_0.01_bound": 0.01 * h.reconstruction_bound,
+            "reconstruction_bound": h.reconstruction_bound,
+            "calibration": h.form_choice,
+        }
+        # e2e: NumPy X in, Y out (H2D and D2H copies inside the timed region)
+        xh = np.ascontiguousarray(x)
+        pf.matmul(xh)
+        t0 = time.perf_counter()
+        ne = max(3, min(args.e2e_steps, 20))
+        for _ in range(ne):
+            yh = pf.matmul(xh)
+        e2e = (time.perf_counter() - t0) / ne
+        out["e2e"] = {"value": round(rhs / e2e, 1), "unit": "RHS/s", "h2d_bytes_per_step": int(xh.nbytes),
+                      "d2h_bytes_per_step": int(yh.nbytes), "ms_per_step": round(1e3 * e2e, 4),
+                      "transfer": "pageable NumPy X copied to the device, Y copied back, per call"}
+        if not args.no_cpu_baseline:
+            from oracle import oracle
+
+            om = oracle.OracleMatrix(data)
+            threads = os.cpu_count() or 1
+            xs = np.ascontiguousarray(x[:, :2])
+            om.matmul(xs[:, :1], threads=threads)
+            t0 = time.perf_counter()
+            reps = 0
+            while reps < 1 or time.perf_counter() - t0 < 10.0:
+                om.matmul(xs, threads=threads)
+                reps += 1
+            dt = time.perf_counter() - t0
+            out["cpu_baseline"] = {"value": round(2 * reps / dt, 3), "unit": "RHS/s", "cores": threads,
+                                   "kind": "port",
+                                   "sample": f"{reps} applies of 2 of the 64 columns in {dt:.1f} s ({threads} threads)"}
+        print(json.dumps(out), flush=True)
+    if pg:
+        pg.barrier()
+        pg.destroy_process_group()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -349,6 +552,8 @@ def main():
         raise SystemExit("--warmup must be >= 3")
     if args.impl == "reference":
         return run_reference_arm(args)
+    if args.workload in PRECISION_WORKLOADS:
+        return run_precision(args)
 
     world, rank, local = dist_setup()
     import numpy as np

@@ -210,6 +210,55 @@ QH_API int qh_matrix_reconstruct(const qh_matrix* m, double* out, size_t out_cou
 QH_API int qh_debug_decode(const qh_matrix* m, int side, int32_t* out, size_t out_count,
                            size_t* needed);
 
+/* ---- Precision form: many right-hand sides per code stream (tcgen05) ----
+ *
+ * The reference re-decodes every code once per right-hand-side column
+ * (src/qhmat/core.cpp:377-386) and its CUDA path does the same per thread
+ * (src/qhmat/cuda.cu:64-102).  A qh_pmatrix holds a second resident layout of
+ * the same QHMAT001 image, built for the 5th-generation tensor cores: each
+ * code digit is read once per pass of up to 64 right-hand sides and
+ * multiplied, as an exact f16 operand, by the hi/mid/lo f16 limbs of all of
+ * them (FP32 accumulation in tensor memory); the per-component FP64 scales,
+ * the dense diagonal blocks (three f16 limbs against the x limbs) and the
+ * final y sums are combined in FP64.  Results carry FP32-level rounding
+ * (about 1e-7 relative to the partial sums), not the plain form's ~1e-15:
+ * callers choose this form when that error fits their budget (the Python
+ * layer's gate: max |y_pf - y_plain| per column below 1% of
+ * reconstruction_bound * ||x||_1).  Needs an sm_103 device. */
+typedef struct qh_pmatrix qh_pmatrix;
+
+typedef struct {
+    uint64_t order, components;
+    uint64_t code_bytes, scale_bytes, dense_bytes; /* packed-byte model, as qh_stats */
+    uint64_t stored_q_bytes, stored_p_bytes, stored_dense_bytes; /* digit planes and dense limb tiles */
+    uint64_t device_bytes;
+    uint64_t col_items, row_items, row_slots;
+    uint64_t mma_elements;      /* M x K elements through the MMAs per pass (x N = 3p limbs) */
+    uint64_t launches_per_pass; /* kernels per pass of <= 64 right-hand sides */
+    uint64_t mma_col_elements, mma_row_elements; /* the column and row kernels' shares */
+} qh_pstats;
+
+/* Parse a QHMAT001 image (the checks and messages of qh_matrix_from_qhmat)
+ * and upload the precision-form layout to `device`. */
+QH_API int qh_pmatrix_from_qhmat(const void* bytes, size_t len, int device, qh_pmatrix** out);
+QH_API void qh_pmatrix_destroy(qh_pmatrix* m);
+QH_API int qh_pmatrix_stats(const qh_pmatrix* m, qh_pstats* out);
+/* Device scratch of one qh_pmatmul_device call with `rhs` columns (passes of
+ * 64 columns share it). */
+QH_API size_t qh_pworkspace_bytes(const qh_pmatrix* m, size_t rhs);
+/* y = A x in the precision form: x, y device pointers, row-major order x rhs,
+ * source order (as qh_matmul_device); workspace NULL = a handle-owned buffer
+ * (calls must then not overlap on the GPU); status: QH_STATUS_* bits.
+ * Stream-ordered.  Column chunks of 64 right-hand sides run in turn. */
+QH_API int qh_pmatmul_device(const qh_pmatrix* m, const double* x, double* y, size_t rhs, void* workspace,
+                             size_t workspace_bytes, void* stream, int* status);
+/* The same, recording five caller-created cudaEvent_t around the first pass's
+ * kernels: before the x preparation, before the column kernel, before the
+ * row kernel, before the combine, after it.  Profiling aid. */
+QH_API int qh_pmatmul_device_profiled(const qh_pmatrix* m, const double* x, double* y, size_t rhs,
+                                      void* workspace, size_t workspace_bytes, void* stream, int* status,
+                                      void* const* events5);
+
 /* Test aid for the bounded device waits: one warp on `device` waits at most
  * `polls` (1 .. 2^20) tests on an mbarrier that nothing completes -- no copy
  * is issued -- and records the timeout in a status int exactly as the apply

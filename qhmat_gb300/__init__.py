@@ -7,8 +7,9 @@ once and applied by hand-written sm_103a kernels through the C ABI declared in
 """
 
 from ._lib import LIB_PATH, load_library
-from .matrix import HMatrix, NativeHMatrix
+from .matrix import HMatrix, NativeHMatrix, PrecisionHMatrix, choose_form, precision_gate
 
 cuda_built = True
 
-__all__ = ["HMatrix", "NativeHMatrix", "LIB_PATH", "load_library", "cuda_built"]
+__all__ = ["HMatrix", "NativeHMatrix", "PrecisionHMatrix", "precision_gate", "choose_form", "LIB_PATH", "load_library",
+           "cuda_built"]

@@ -25,6 +25,13 @@ class QhStats(C.Structure):
         "launches_per_apply", "host_direct", "left_code_bytes", "right_code_bytes")]
 
 
+class QhPStats(C.Structure):
+    _fields_ = [(name, C.c_uint64) for name in (
+        "order", "components", "code_bytes", "scale_bytes", "dense_bytes", "stored_q_bytes",
+        "stored_p_bytes", "stored_dense_bytes", "device_bytes", "col_items", "row_items", "row_slots",
+        "mma_elements", "launches_per_pass", "mma_col_elements", "mma_row_elements")]
+
+
 class QhBlockDesc(C.Structure):
     _fields_ = [("row0", C.c_size_t), ("row1", C.c_size_t), ("col0", C.c_size_t),
                 ("col1", C.c_size_t), ("rank", C.c_size_t), ("factor_offset", C.c_size_t),
@@ -77,6 +84,18 @@ def load_library() -> C.CDLL:
     lib.qh_fnv1a64.argtypes = [C.c_char_p, sz]
     lib.qh_debug_decode.restype = i32
     lib.qh_debug_decode.argtypes = [vp, i32, vp, sz, C.POINTER(sz)]
+    lib.qh_pmatrix_from_qhmat.restype = i32
+    lib.qh_pmatrix_from_qhmat.argtypes = [C.c_char_p, sz, i32, C.POINTER(vp)]
+    lib.qh_pmatrix_destroy.restype = None
+    lib.qh_pmatrix_destroy.argtypes = [vp]
+    lib.qh_pmatrix_stats.restype = i32
+    lib.qh_pmatrix_stats.argtypes = [vp, C.POINTER(QhPStats)]
+    lib.qh_pworkspace_bytes.restype = sz
+    lib.qh_pworkspace_bytes.argtypes = [vp, sz]
+    lib.qh_pmatmul_device.restype = i32
+    lib.qh_pmatmul_device.argtypes = [vp, vp, vp, sz, vp, sz, vp, vp]
+    lib.qh_pmatmul_device_profiled.restype = i32
+    lib.qh_pmatmul_device_profiled.argtypes = [vp, vp, vp, sz, vp, sz, vp, vp, vp]
     lib.qh_debug_wait_timeout.restype = i32
     lib.qh_debug_wait_timeout.argtypes = [i32, i32]
     lib.qh_matrix_reconstruct.restype = i32

@@ -50,6 +50,7 @@
 #include <unistd.h>
 
 #include "../../include/qhmat_gb300.h"
+#include "errors.hpp"
 #include "layout.hpp"
 
 namespace qhg {
@@ -1312,6 +1313,10 @@ int cuda_fail(cudaError_t e, const char* what) {
 size_t align256(size_t v) { return (v + 255) & ~size_t(255); }
 
 }  // namespace
+
+// Shared with the other translation units of the library (errors.hpp).
+int set_error(int code, const std::string& msg) { return fail(code, msg); }
+
 }  // namespace qhg
 
 using namespace qhg;

@@ -1,0 +1,1104 @@
+// GB300 (sm_103a) precision form of the quantized H-matrix apply: many
+// right-hand sides at once on the 5th-generation tensor cores.
+//
+// The plain apply (matvec.cu) streams every code once per right-hand side.
+// Here each code digit is streamed once per pass of up to 64 right-hand sides
+// and multiplied, as an f16 operand, against all of them at once with
+// tcgen05.mma (M = 128, K = 16 per instruction, N = 3p: hi/mid/lo f16 limbs
+// of every right-hand side), accumulating in FP32 in tensor memory:
+//
+//   pf_xmax / pf_xlimbs  x (source order) -> one exponent per column; x' = x
+//                        2^(1037-E) split into three f16 limbs, stored as the
+//                        rows 3r + l of XT (clustered entry order), read by
+//                        2-D tensor copies (cp.async.bulk.tensor, 128-byte
+//                        swizzle) straight into the B operand layout;
+//   pf_column_kernel     T = Q^T X' for 128 components sharing a column range;
+//                        u = (s^P s^Q) T in FP64 (the per-component scale),
+//                        stored as FP32 per row-side slot;
+//   pf_row_kernel        y = P U' per 128-row tile (U' = three f16 limbs of u
+//                        on a per-column exponent), plus the dense diagonal
+//                        blocks as three f16 limb tiles against X' limbs;
+//                        FP64 partial sums per K split;
+//   pf_combine_kernel    y = the partials of each tile summed in FP64, in
+//                        order (deterministic), scattered through perm.
+//
+// Both streaming kernels are persistent and warp-specialised: one warp issues
+// the bulk and tensor copies into a ring of shared-memory stages, six warps
+// turn digit bytes (and U) into f16 operand tiles, one thread issues the
+// MMAs, four warps drain the accumulators from tensor memory.  Every wait is
+// bounded; a wait that gives up sets QH_STATUS_TIMEOUT and the block winds
+// down (after a bounded drain of its copies and MMAs) instead of hanging.
+//
+// Accuracy: every digit x limb product is exact; sums are FP32 (relative
+// error ~2^-24 of the partial sums), x and u carry ~33 bits in their limbs.
+// This form is checked against the plain FP64 form and the dense product.
+#include <cuda.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/qhmat_gb300.h"
+#include "errors.hpp"
+#include "layout.hpp"
+#include "pf_layout.hpp"
+
+namespace qhg {
+namespace pf {
+
+constexpr int kThreads = 384;     // 12 warps
+constexpr int kConvWarp0 = 2;     // warps 2..7 convert
+constexpr int kConvWarps = 6;
+constexpr int kEpiWarp0 = 8;      // warps 8..11 drain tensor memory (lane quarters 0..3)
+constexpr int kAStages = 4;
+constexpr int kBStages = 2;
+constexpr int kNMax = 192;        // N of one pass (3 limbs x 64 right-hand sides)
+constexpr int kBTileBytes = kNMax * 128;   // B operand stage (N rows of 64 f16)
+constexpr int kURawBytes = kPfK * kPfMaxRhs * 4;  // 64 slots of FP32 u
+constexpr int kWaitLimit = 1 << 22;
+// K chunks one accumulation segment spans.  The tensor cores add each MMA's
+// products into the FP32 accumulator with truncation, so the error of an
+// accumulator grows with its number of MMAs (measured: relative error
+// proportional to the chain length); segments of a few chunks are drained
+// into round-to-nearest FP32 registers by the epilogue warps, from two
+// alternating tensor-memory buffers (columns 0 and 256).
+constexpr int kSegChunks = 4;
+constexpr int kAccStride = 256;
+constexpr int kStatusNonfinite = QH_STATUS_NONFINITE;
+constexpr int kStatusTimeout = QH_STATUS_TIMEOUT;
+
+// Shared-memory map of both kernels (offsets from a 1024-byte-aligned base).
+constexpr int kOffAF16 = 0;                                    // 4 x 16 KB f16 A tiles
+constexpr int kOffBF16 = kOffAF16 + kAStages * kPfTileBytes;   // 2 x 24 KB f16 B tiles
+constexpr int kOffARaw = kOffBF16 + kBStages * kBTileBytes;    // 4 x 8 KB digit planes
+constexpr int kOffBRaw = kOffARaw + kAStages * kPfPlaneBytes;  // 2 x 16 KB FP32 u (row kernel)
+constexpr int kSmemColumn = kOffBRaw + 1024;                   // + alignment slack
+constexpr int kSmemRow = kOffBRaw + kBStages * kURawBytes + 1024;
+
+struct Arena {
+    const int32_t* perm;
+    const PfColItem* col_items;
+    const PfComp* comps;
+    const int32_t* dests;
+    const PfRowItem* row_items;
+    const PfRowChunk* chunks;
+    const int32_t* col_sched;
+    const int32_t* row_sched;
+    const uint8_t* qraw;
+    const uint8_t* praw;
+};
+
+struct Work {
+    int* ex;       // [64] exponent field of max |x| per right-hand side
+    int* eu;       // [64] exponent field of max |u| per right-hand side
+    __half* xt;    // [N][n_ent] f16 limbs of x' (row 3r + l)
+    float* ut;     // [n_slots][pu] u per row-side slot
+    double* part;  // [n_parts][128][pu] FP64 partial sums of the row side
+};
+
+// ------------------------------------------------------------ primitives
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return uint32_t(__cvta_generic_to_shared(p)); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_expect(uint64_t* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint64_t* bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait; gives up when the block has been told to abort, or after
+// kWaitLimit tests (then it raises the abort flag and the timeout bit).
+__device__ __forceinline__ bool wait_bar(uint64_t* bar, unsigned parity, volatile int* abort_flag, int* status) {
+    for (int i = 0; i < kWaitLimit; ++i) {
+        if (mbar_try(bar, parity)) return true;
+        if ((i & 255) == 255 && *abort_flag) return false;
+    }
+    *abort_flag = 1;
+    if (status) atomicOr(status, kStatusTimeout);
+    return false;
+}
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+// 2-D tensor copy of the box at (x, y) of a tensor map into shared memory.
+__device__ __forceinline__ void tma_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+            smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// Tensor memory: allocate / free `cols` columns (one warp), the address
+// written to shared memory.
+__device__ __forceinline__ void tmem_alloc(uint32_t* dst, unsigned cols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst)), "r"(cols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_free(uint32_t taddr, unsigned cols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(cols) : "memory");
+}
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+
+// Shared-memory matrix descriptor of a K-major operand in the 128-byte
+// swizzled layout: rows of 128 bytes, 8-row groups 1024 bytes apart (stride
+// byte offset), start advanced by 32 bytes per K step of 16 f16.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t addr) {
+    uint64_t d = 0;
+    d |= uint64_t((addr & 0x3FFFFu) >> 4);
+    d |= uint64_t(16 >> 4) << 16;    // leading byte offset (unused for swizzled K-major)
+    d |= uint64_t(1024 >> 4) << 32;  // stride byte offset
+    d |= uint64_t(1) << 46;          // descriptor version
+    d |= uint64_t(2) << 61;          // 128-byte swizzle
+    return d;
+}
+// Instruction descriptor: f16 x f16 -> f32, both K-major, M = 128, N.
+__host__ __device__ constexpr uint32_t mma_idesc(int n) {
+    return (1u << 4) | (uint32_t(n >> 3) << 17) | (uint32_t(128 >> 4) << 24);
+}
+__device__ __forceinline__ void mma_f16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, int accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+// Arrive on `bar` when every MMA this thread issued so far has completed.
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+// 16 consecutive FP32 columns of this warp's 32 tensor-memory lanes.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr)
+        : "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+__device__ __forceinline__ uint32_t prmt(uint32_t a, uint32_t b, uint32_t sel) {
+    uint32_t r;
+    asm("prmt.b32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(sel));
+    return r;
+}
+__device__ __forceinline__ uint32_t hsub2(uint32_t a, uint32_t b) {
+    uint32_t r;
+    asm("sub.f16x2 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b));
+    return r;
+}
+
+// Byte offset of 16-byte chunk c (elements 8c .. 8c+7) of row r in a 128-row
+// x 64-f16 tile, 128-byte swizzle.
+__device__ __forceinline__ uint32_t swz_chunk(int r, int c) {
+    return uint32_t((r >> 3) * 1024 + (r & 7) * 128 + ((c ^ (r & 7)) << 4));
+}
+
+// Eight digit bytes of plane m (top plane signed) -> eight f16 values
+// d 2^(E-25) for exponent field E: the f16 with exponent field E and mantissa
+// bits d is 2^(E-15) + d 2^(E-25); subtracting 2^(E-15) leaves the digit's
+// value exactly (a subnormal when E = 1).  The signed top digit is biased by
+// 128 first.
+__device__ __forceinline__ uint4 digits_to_f16(uint2 w, uint32_t eb, uint32_t sub, bool top) {
+    if (top) {
+        w.x ^= 0x80808080u;
+        w.y ^= 0x80808080u;
+    }
+    return make_uint4(hsub2(prmt(w.x, eb, 0x4140u), sub), hsub2(prmt(w.x, eb, 0x4342u), sub),
+                      hsub2(prmt(w.y, eb, 0x4140u), sub), hsub2(prmt(w.y, eb, 0x4342u), sub));
+}
+
+// Convert one digit plane (rows stored with 64 bytes each) into an f16 A
+// tile, digits of plane m weighted 2^(8m + 1 + ebias - 25): the column side
+// uses ebias = 0 (plane m at 2^(8m-24)), the row side 24 - 8(P-1) (top plane at
+// 2^0).  half 0: 128 stored rows; half 1: stored rows are tile rows 0..63
+// (64..127 zero); half 2: stored rows are tile rows 64..127 (0..63 zero).
+__device__ __forceinline__ void convert_plane(const uint8_t* raw, uint8_t* tile, int m, int P, int ebias, int half,
+                                              int ctid, int nthreads) {
+    const uint32_t E = uint32_t(8 * m + 1 + ebias);
+    const uint32_t eb = (E << 2) * 0x01010101u;
+    const bool top = m == P - 1;
+    const uint32_t sub = ((E << 10) | (top ? 0x80u : 0u)) * 0x00010001u;
+    for (int idx = ctid; idx < 1024; idx += nthreads) {
+        const int r = idx >> 3, c = idx & 7;
+        uint4 v;
+        const int sr = half == 0 ? r : (half == 1 ? (r < 64 ? r : -1) : (r >= 64 ? r - 64 : -1));
+        if (sr >= 0) {
+            const uint2 w = *reinterpret_cast<const uint2*>(raw + sr * 64 + c * 8);
+            v = digits_to_f16(w, eb, sub, top);
+        } else {
+            v = make_uint4(0u, 0u, 0u, 0u);
+        }
+        *reinterpret_cast<uint4*>(tile + swz_chunk(r, c)) = v;
+    }
+}
+
+__device__ __forceinline__ uint32_t pack_h2(__half a, __half b) {
+    return uint32_t(__half_as_ushort(a)) | (uint32_t(__half_as_ushort(b)) << 16);
+}
+
+// U of 64 slots (FP32, row stride pu) -> the f16 B tile: row 3r + l holds limb
+// l of u' = u 2^k[r] 256^(P-1) for the 64 slots of a chunk with P planes
+// (slots >= nvalid: 0).
+__device__ __forceinline__ void convert_u(const float* raw, uint8_t* tile, int p, int pu, int nvalid, int P,
+                                          const float* scale, int ctid, int nthreads) {
+    const float pw = __int_as_float((127 + 8 * (P - 1)) << 23);  // 256^(P-1)
+    for (int idx = ctid; idx < p * 8; idx += nthreads) {
+        const int r = idx % p, kg = idx / p;
+        const float sc = scale[r] * pw;
+        uint32_t h[3][4];
+#pragma unroll
+        for (int s = 0; s < 8; s += 2) {
+            __half lm[2][3];
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+                const int k = 8 * kg + s + q;
+                const float u = k < nvalid ? raw[k * pu + r] * sc : 0.0f;
+                const __half a = __float2half_rn(u);
+                const float r1 = u - __half2float(a);
+                const __half b = __float2half_rn(r1);
+                const float r2 = r1 - __half2float(b);
+                lm[q][0] = a;
+                lm[q][1] = b;
+                lm[q][2] = __float2half_rn(r2);
+            }
+#pragma unroll
+            for (int l = 0; l < 3; ++l) h[l][s >> 1] = pack_h2(lm[0][l], lm[1][l]);
+        }
+#pragma unroll
+        for (int l = 0; l < 3; ++l)
+            *reinterpret_cast<uint4*>(tile + swz_chunk(3 * r + l, kg)) = make_uint4(h[l][0], h[l][1], h[l][2], h[l][3]);
+    }
+}
+
+
+// Shared state of one block.
+struct Shared {
+    uint64_t a_full[kAStages], a_conv[kAStages], a_empty[kAStages];
+    uint64_t b_full[kBStages], b_conv[kBStages], b_empty[kBStages];
+    uint64_t acc_full[2], acc_empty[2];
+    uint64_t drain;
+    uint32_t tmem;
+    int abort_flag;
+    int ex[kPfMaxRhs];
+    int eu_max[kPfMaxRhs];  // column kernel: this block's max exponent of u
+    int ku[kPfMaxRhs];      // row kernel: U' = u 2^ku
+    float uscale[kPfMaxRhs];
+    float fxscale[kPfMaxRhs];  // column kernel: 2^(24 + E_r - 1037)
+    float flscale[kPfMaxRhs];  // row kernel: 2^-ku (low-rank sums)
+    float fdscale[kPfMaxRhs];  // row kernel: 2^(E_r - 1037) (dense sums, times 2^dense_exp)
+};
+
+__device__ __forceinline__ void init_barriers(Shared& S) {
+    for (int i = 0; i < kAStages; ++i) {
+        mbar_init(&S.a_full[i], 1);
+        mbar_init(&S.a_conv[i], kConvWarps);
+        mbar_init(&S.a_empty[i], 1);
+    }
+    for (int i = 0; i < kBStages; ++i) {
+        mbar_init(&S.b_full[i], 1);
+        mbar_init(&S.b_conv[i], kConvWarps);
+        mbar_init(&S.b_empty[i], 1);
+    }
+    for (int i = 0; i < 2; ++i) {
+        mbar_init(&S.acc_full[i], 1);
+        mbar_init(&S.acc_empty[i], 4);
+    }
+    mbar_init(&S.drain, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// ------------------------------------------------------------ prep kernels
+
+// Largest exponent field of each right-hand-side column (and the nonfinite
+// flag): block b, thread r reads rows 256b .. 256b+255 of column r.
+__global__ void __launch_bounds__(64) pf_xmax_kernel(const double* __restrict__ x, long long ld, int n, int p,
+                                                     int* ex, int* status) {
+    const int r = threadIdx.x;
+    if (r >= p) return;
+    int m = 0;
+    bool bad = false;
+    const int i1 = min(n, (blockIdx.x + 1) * 256);
+    for (int i = blockIdx.x * 256; i < i1; ++i) {
+        const double v = x[(long long)i * ld + r];
+        const int e = int((__double_as_longlong(v) >> 52) & 0x7FF);
+        bad |= e == 0x7FF;
+        m = max(m, e == 0x7FF ? 0 : e);
+    }
+    if (bad && status) atomicOr(status, kStatusNonfinite);
+    atomicMax(ex + r, m);
+}
+
+// XT[3r + l][i] = limb l of x'(perm[i], r) = x 2^(1037 - E_r); rows 3p .. N-1
+// and entries n .. n_ent-1 are zero.
+__global__ void __launch_bounds__(256) pf_xlimbs_kernel(const double* __restrict__ x, long long ld, int n, int p,
+                                                        int n_ent, int N, const int32_t* __restrict__ perm,
+                                                        const int* __restrict__ ex, __half* __restrict__ xt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_ent) return;
+    const long long src = i < n ? (long long)__ldg(perm + i) : -1;
+    for (int r = 0; r < p; ++r) {
+        const int E = ex[r];
+        double v = src >= 0 && E ? x[src * ld + r] : 0.0;
+        if (!isfinite(v)) v = 0.0;
+        v = scalbn(v, 1037 - E);
+        const __half a = __double2half(v);
+        const double r1 = v - double(__half2float(a));
+        const __half b = __double2half(r1);
+        const double r2 = r1 - double(__half2float(b));
+        xt[(long long)(3 * r) * n_ent + i] = a;
+        xt[(long long)(3 * r + 1) * n_ent + i] = b;
+        xt[(long long)(3 * r + 2) * n_ent + i] = __double2half(r2);
+    }
+    for (int row = 3 * p; row < N; ++row) xt[(long long)row * n_ent + i] = __ushort_as_half(0);
+}
+
+// ------------------------------------------------------------ column kernel
+
+// Persistent: block g runs column items col_sched[g] .. col_sched[g+1].
+__global__ void __launch_bounds__(kThreads, 1) pf_column_kernel(Arena A, Work W, const __grid_constant__ CUtensorMap xmap,
+                                                                int p, int N, int pu, int* status) {
+    extern __shared__ uint8_t smem_dyn[];
+    uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_dyn) + 1023) & ~uintptr_t(1023));
+    __shared__ Shared S;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int it0 = __ldg(A.col_sched + blockIdx.x), it1 = __ldg(A.col_sched + blockIdx.x + 1);
+    if (tid == 0) {
+        init_barriers(S);
+        S.abort_flag = 0;
+    }
+    if (tid < kPfMaxRhs) {
+        const int E = tid < p ? W.ex[tid] : 0;
+        S.ex[tid] = E;
+        S.eu_max[tid] = 0;
+        S.fxscale[tid] = E ? ldexpf(1.0f, max(-126, min(127, 24 + E - 1037))) : 0.0f;
+    }
+    if (warp == 1) tmem_alloc(&S.tmem, 512);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = S.tmem;
+    volatile int* abort_flag = &S.abort_flag;
+
+    if (warp == 0) {
+        // ---- producer
+        if (lane == 0) {
+            unsigned ai = 0, bi = 0;
+            bool ok = true;
+            for (int it = it0; it < it1 && ok; ++it) {
+                const PfColItem I = A.col_items[it];
+                for (int kc = 0; kc < I.nkc && ok; ++kc) {
+                    const int sb = bi % kBStages;
+                    if (bi >= kBStages) ok = wait_bar(&S.b_empty[sb], ((bi / kBStages) - 1) & 1, abort_flag, status);
+                    if (!ok) break;
+                    mbar_expect(&S.b_full[sb], unsigned(N * 128));
+                    tma_2d(sm + kOffBF16 + sb * kBTileBytes, &xmap, I.e_base + kc * kPfK, 0, &S.b_full[sb]);
+                    ++bi;
+                    for (int m = 0; m < I.planes; ++m) {
+                        const int sa = ai % kAStages;
+                        if (ai >= kAStages) ok = wait_bar(&S.a_empty[sa], ((ai / kAStages) - 1) & 1, abort_flag, status);
+                        if (!ok) break;
+                        mbar_expect(&S.a_full[sa], kPfPlaneBytes);
+                        bulk_g2s(sm + kOffARaw + sa * kPfPlaneBytes,
+                                 A.qraw + I.a_off + (long long)(kc * I.planes + m) * kPfPlaneBytes, kPfPlaneBytes,
+                                 &S.a_full[sa]);
+                        ++ai;
+                    }
+                }
+            }
+            // copies still in flight after an abort: wait for them (bounded)
+            if (!ok) {
+                for (unsigned k = ai > kAStages ? ai - kAStages : 0; k < ai; ++k)
+                    for (int i = 0; i < kWaitLimit && !mbar_try(&S.a_full[k % kAStages], (k / kAStages) & 1); ++i) {}
+                for (unsigned k = bi > kBStages ? bi - kBStages : 0; k < bi; ++k)
+                    for (int i = 0; i < kWaitLimit && !mbar_try(&S.b_full[k % kBStages], (k / kBStages) & 1); ++i) {}
+            }
+        }
+    } else if (warp == 1) {
+        // ---- MMA issuer: per item, segments of kSegChunks K chunks, each into
+        // the next of two accumulator buffers
+        if (lane == 0) {
+            const uint32_t idesc = mma_idesc(N);
+            unsigned ai = 0, bi = 0, seg = 0;
+            bool ok = true;
+            for (int it = it0; it < it1 && ok; ++it) {
+                const PfColItem I = A.col_items[it];
+                for (int kc0 = 0; kc0 < I.nkc && ok; kc0 += kSegChunks, ++seg) {
+                    const int buf = seg & 1;
+                    if (seg >= 2) ok = wait_bar(&S.acc_empty[buf], ((seg >> 1) - 1) & 1, abort_flag, status);
+                    if (!ok) break;
+                    tc_fence_after();
+                    const uint32_t d = tmem + uint32_t(buf * kAccStride);
+                    int acc = 0;
+                    for (int kc = kc0; kc < min(I.nkc, kc0 + kSegChunks) && ok; ++kc) {
+                        const int sb = bi % kBStages;
+                        ok = wait_bar(&S.b_full[sb], (bi / kBStages) & 1, abort_flag, status);
+                        if (!ok) break;
+                        const uint32_t b_addr = smem_u32(sm + kOffBF16 + sb * kBTileBytes);
+                        for (int m = 0; m < I.planes; ++m) {
+                            const int sa = ai % kAStages;
+                            ok = wait_bar(&S.a_conv[sa], (ai / kAStages) & 1, abort_flag, status);
+                            if (!ok) break;
+                            tc_fence_after();
+                            const uint32_t a_addr = smem_u32(sm + kOffAF16 + sa * kPfTileBytes);
+#pragma unroll
+                            for (int ks = 0; ks < 4; ++ks) {
+                                mma_f16(d, sw128_desc(a_addr + 32 * ks), sw128_desc(b_addr + 32 * ks), idesc, acc);
+                                acc = 1;
+                            }
+                            mma_commit(&S.a_empty[sa]);
+                            ++ai;
+                        }
+                        mma_commit(&S.b_empty[sb]);
+                        ++bi;
+                    }
+                    mma_commit(&S.acc_full[buf]);
+                }
+            }
+            // every MMA issued has finished before tensor memory is freed
+            mma_commit(&S.drain);
+            for (int i = 0; i < kWaitLimit && !mbar_try(&S.drain, 0); ++i) {}
+        }
+    } else if (warp < kEpiWarp0) {
+        // ---- converters: digit planes -> f16 A tiles
+        const int ctid = tid - kConvWarp0 * 32, nct = kConvWarps * 32;
+        unsigned ai = 0;
+        bool ok = true;
+        for (int it = it0; it < it1 && ok; ++it) {
+            const PfColItem I = A.col_items[it];
+            for (int kc = 0; kc < I.nkc && ok; ++kc)
+                for (int m = 0; m < I.planes; ++m) {
+                    const int sa = ai % kAStages;
+                    ok = wait_bar(&S.a_full[sa], (ai / kAStages) & 1, abort_flag, status);
+                    if (!ok) break;
+                    convert_plane(sm + kOffARaw + sa * kPfPlaneBytes, sm + kOffAF16 + sa * kPfTileBytes, m, I.planes,
+                                  0, 0, ctid, nct);
+                    fence_async_smem();
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(&S.a_conv[sa]);
+                    ++ai;
+                }
+        }
+    } else {
+        // ---- epilogue: T summed over the item's segments in FP32 registers,
+        // then u = s T 2^(24 + E_r - 1037) per component and column, in FP32
+        // (u is stored as FP32; the FP64 pipe of this part would take ~20 us
+        // per item for the same work)
+        const int q = warp & 3, j = 32 * q + lane;
+        unsigned seg = 0;
+        bool ok = true;
+        for (int it = it0; it < it1 && ok; ++it) {
+            const PfColItem I = A.col_items[it];
+            PfComp C{};
+            if (j < I.count) C = A.comps[I.comp0 + j];
+            const float sf = float(C.scale);
+            float t[kPfMaxRhs];
+#pragma unroll
+            for (int r = 0; r < kPfMaxRhs; ++r) t[r] = 0.0f;
+            for (int kc0 = 0; kc0 < I.nkc; kc0 += kSegChunks, ++seg) {
+                const int buf = seg & 1;
+                if (!(ok = wait_bar(&S.acc_full[buf], (seg >> 1) & 1, abort_flag, status))) break;
+                tc_fence_after();
+                const uint32_t base = tmem + (uint32_t(32 * q) << 16) + uint32_t(buf * kAccStride);
+#pragma unroll
+                for (int g = 0; g < kPfMaxRhs / 16; ++g) {
+                    if (16 * g >= p) break;
+                    float v0[16], v1[16], v2[16];
+                    tmem_ld16(base + 48 * g, v0);
+                    tmem_ld16(base + 48 * g + 16, v1);
+                    tmem_ld16(base + 48 * g + 32, v2);
+                    tmem_wait_ld();
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) {
+                        // columns 3i, 3i+1, 3i+2 of the 48: the limbs of right-hand side 16g + i
+                        const int c0 = 3 * i, c1 = 3 * i + 1, c2 = 3 * i + 2;
+                        const float a0 = c0 < 16 ? v0[c0] : (c0 < 32 ? v1[c0 - 16] : v2[c0 - 32]);
+                        const float a1 = c1 < 16 ? v0[c1] : (c1 < 32 ? v1[c1 - 16] : v2[c1 - 32]);
+                        const float a2 = c2 < 16 ? v0[c2] : (c2 < 32 ? v1[c2 - 16] : v2[c2 - 32]);
+                        t[16 * g + i] += (a0 + a1) + a2;
+                    }
+                }
+                // accumulator drained: release it to the MMA warp
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&S.acc_empty[buf]);
+            }
+            if (!ok) break;
+            int emax = 0;  // largest shift 8(P-1) over this component's destinations
+            for (int d = 0; d < (j < I.count ? C.ndest : 0); ++d) emax = max(emax, 8 * (__ldg(A.dests + C.dest0 + d) >> 28));
+#pragma unroll
+            for (int g = 0; g < kPfMaxRhs / 16; ++g) {
+                if (16 * g >= p) break;
+                float u[16];
+#pragma unroll
+                for (int i = 0; i < 16; ++i) {
+                    const int r = 16 * g + i;
+                    u[i] = (j < I.count && r < p) ? t[r] * sf * S.fxscale[r] : 0.0f;
+                }
+                for (int d = 0; d < (j < I.count ? C.ndest : 0); ++d) {
+                    const int slot = __ldg(A.dests + C.dest0 + d) & 0x0FFFFFFF;
+                    float4* dst = reinterpret_cast<float4*>(W.ut + (long long)slot * pu + 16 * g);
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) dst[k] = make_float4(u[4 * k], u[4 * k + 1], u[4 * k + 2], u[4 * k + 3]);
+                }
+                // largest exponent of u 256^(P-1) per column over the warp
+#pragma unroll
+                for (int i = 0; i < 16; ++i) {
+                    const int e = int((__float_as_uint(u[i]) >> 23) & 0xFF);
+                    const int m = __reduce_max_sync(0xFFFFFFFFu, e ? e + emax : 0);
+                    if (lane == 0 && m) atomicMax(&S.eu_max[16 * g + i], m);
+                }
+            }
+        }
+    }
+    __syncthreads();
+    if (tid < p && S.eu_max[tid]) atomicMax(W.eu + tid, S.eu_max[tid] + 1023 - 127);
+    tc_fence_after();
+    if (warp == 1) tmem_free(tmem, 512);
+}
+
+// ------------------------------------------------------------ row kernel
+
+__global__ void __launch_bounds__(kThreads, 1) pf_row_kernel(Arena A, Work W, const __grid_constant__ CUtensorMap xmap,
+                                                             int p, int N, int pu, int* status) {
+    extern __shared__ uint8_t smem_dyn[];
+    uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_dyn) + 1023) & ~uintptr_t(1023));
+    __shared__ Shared S;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int it0 = __ldg(A.row_sched + blockIdx.x), it1 = __ldg(A.row_sched + blockIdx.x + 1);
+    if (tid == 0) {
+        init_barriers(S);
+        S.abort_flag = 0;
+    }
+    if (tid < kPfMaxRhs) {
+        const int E = tid < p ? W.ex[tid] : 0;
+        S.ex[tid] = E;
+        S.fdscale[tid] = E ? ldexpf(1.0f, max(-126, min(127, E - 1037))) : 0.0f;
+        const int eu = tid < p ? W.eu[tid] : 0;
+        const int k = eu ? max(-126, min(127, 1037 - eu)) : 0;
+        S.ku[tid] = k;
+        S.uscale[tid] = eu ? ldexpf(1.0f, k) : 0.0f;
+        S.flscale[tid] = eu ? ldexpf(1.0f, -k) : 0.0f;
+    }
+    // B rows 3p .. N-1 of both f16 B stages stay zero (the converters write
+    // only rows < 3p; tensor copies of x write zeros there)
+    for (int idx = tid; idx < kBStages * (N - 3 * p) * 8; idx += kThreads) {
+        const int s = idx / ((N - 3 * p) * 8), rest = idx % ((N - 3 * p) * 8);
+        const int row = 3 * p + rest / 8, c = rest % 8;
+        *reinterpret_cast<uint4*>(sm + kOffBF16 + s * kBTileBytes + swz_chunk(row, c)) = make_uint4(0u, 0u, 0u, 0u);
+    }
+    fence_async_smem();
+    if (warp == 1) tmem_alloc(&S.tmem, 512);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = S.tmem;
+    volatile int* abort_flag = &S.abort_flag;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            unsigned ai = 0, bi = 0;
+            bool ok = true;
+            for (int it = it0; it < it1 && ok; ++it) {
+                const PfRowItem I = A.row_items[it];
+                for (int c = 0; c < I.nchunks && ok; ++c) {
+                    const PfRowChunk C = A.chunks[I.chunk0 + c];
+                    const int sb = bi % kBStages;
+                    if (bi >= kBStages) ok = wait_bar(&S.b_empty[sb], ((bi / kBStages) - 1) & 1, abort_flag, status);
+                    if (!ok) break;
+                    if (C.kind == 0) {
+                        const unsigned bytes = unsigned(kPfK * pu * 4);
+                        mbar_expect(&S.b_full[sb], bytes);
+                        bulk_g2s(sm + kOffBRaw + sb * kURawBytes, W.ut + (long long)C.b * pu, bytes, &S.b_full[sb]);
+                    } else {
+                        mbar_expect(&S.b_full[sb], unsigned(N * 128));
+                        tma_2d(sm + kOffBF16 + sb * kBTileBytes, &xmap, C.b, 0, &S.b_full[sb]);
+                    }
+                    ++bi;
+                    const int nt = C.kind == 0 ? C.planes : 3;
+                    const unsigned pbytes = C.kind == 0 ? unsigned((C.half == 0 ? 128 : 64) * kPfK) : unsigned(kPfTileBytes);
+                    for (int m = 0; m < nt; ++m) {
+                        const int sa = ai % kAStages;
+                        if (ai >= kAStages) ok = wait_bar(&S.a_empty[sa], ((ai / kAStages) - 1) & 1, abort_flag, status);
+                        if (!ok) break;
+                        mbar_expect(&S.a_full[sa], pbytes);
+                        uint8_t* dst = C.kind == 0 ? sm + kOffARaw + sa * kPfPlaneBytes : sm + kOffAF16 + sa * kPfTileBytes;
+                        bulk_g2s(dst, A.praw + C.a_off + (long long)m * pbytes, pbytes, &S.a_full[sa]);
+                        ++ai;
+                    }
+                }
+            }
+            if (!ok) {
+                for (unsigned k = ai > kAStages ? ai - kAStages : 0; k < ai; ++k)
+                    for (int i = 0; i < kWaitLimit && !mbar_try(&S.a_full[k % kAStages], (k / kAStages) & 1); ++i) {}
+                for (unsigned k = bi > kBStages ? bi - kBStages : 0; k < bi; ++k)
+                    for (int i = 0; i < kWaitLimit && !mbar_try(&S.b_full[k % kBStages], (k / kBStages) & 1); ++i) {}
+            }
+        }
+    } else if (warp == 1) {
+        // ---- MMA issuer: per item, segments of up to kSegChunks chunks of one
+        // kind (low rank or dense), each into the next of two buffers
+        if (lane == 0) {
+            const uint32_t idesc = mma_idesc(N);
+            unsigned ai = 0, bi = 0, seg = 0;
+            bool ok = true;
+            for (int it = it0; it < it1 && ok; ++it) {
+                const PfRowItem I = A.row_items[it];
+                int c = 0;
+                while (c < I.nchunks && ok) {
+                    const int kind = A.chunks[I.chunk0 + c].kind;
+                    int c_end = c + 1;
+                    while (c_end < I.nchunks && c_end - c < kSegChunks && A.chunks[I.chunk0 + c_end].kind == kind)
+                        ++c_end;
+                    const int buf = seg & 1;
+                    if (seg >= 2) ok = wait_bar(&S.acc_empty[buf], ((seg >> 1) - 1) & 1, abort_flag, status);
+                    if (!ok) break;
+                    tc_fence_after();
+                    const uint32_t d = tmem + uint32_t(buf * kAccStride);
+                    int acc = 0;
+                    for (; c < c_end && ok; ++c) {
+                        const PfRowChunk C = A.chunks[I.chunk0 + c];
+                        const int sb = bi % kBStages;
+                        ok = wait_bar(&S.b_conv[sb], (bi / kBStages) & 1, abort_flag, status);
+                        if (!ok) break;
+                        const uint32_t b_addr = smem_u32(sm + kOffBF16 + sb * kBTileBytes);
+                        const int nt = C.kind == 0 ? C.planes : 3;
+                        for (int m = 0; m < nt; ++m) {
+                            const int sa = ai % kAStages;
+                            ok = wait_bar(&S.a_conv[sa], (ai / kAStages) & 1, abort_flag, status);
+                            if (!ok) break;
+                            tc_fence_after();
+                            const uint32_t a_addr = smem_u32(sm + kOffAF16 + sa * kPfTileBytes);
+#pragma unroll
+                            for (int ks = 0; ks < 4; ++ks) {
+                                mma_f16(d, sw128_desc(a_addr + 32 * ks), sw128_desc(b_addr + 32 * ks), idesc, acc);
+                                acc = 1;
+                            }
+                            mma_commit(&S.a_empty[sa]);
+                            ++ai;
+                        }
+                        mma_commit(&S.b_empty[sb]);
+                        ++bi;
+                    }
+                    mma_commit(&S.acc_full[buf]);
+                    ++seg;
+                }
+            }
+            mma_commit(&S.drain);
+            for (int i = 0; i < kWaitLimit && !mbar_try(&S.drain, 0); ++i) {}
+        }
+    } else if (warp < kEpiWarp0) {
+        const int ctid = tid - kConvWarp0 * 32, nct = kConvWarps * 32;
+        unsigned ai = 0, bi = 0;
+        bool ok = true;
+        for (int it = it0; it < it1 && ok; ++it) {
+            const PfRowItem I = A.row_items[it];
+            for (int c = 0; c < I.nchunks && ok; ++c) {
+                const PfRowChunk C = A.chunks[I.chunk0 + c];
+                const int sb = bi % kBStages;
+                ok = wait_bar(&S.b_full[sb], (bi / kBStages) & 1, abort_flag, status);
+                if (!ok) break;
+                if (C.kind == 0)
+                    convert_u(reinterpret_cast<const float*>(sm + kOffBRaw + sb * kURawBytes),
+                              sm + kOffBF16 + sb * kBTileBytes, p, pu, C.nvalid, C.planes, S.uscale, ctid, nct);
+                fence_async_smem();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&S.b_conv[sb]);
+                ++bi;
+                const int nt = C.kind == 0 ? C.planes : 3;
+                for (int m = 0; m < nt; ++m) {
+                    const int sa = ai % kAStages;
+                    ok = wait_bar(&S.a_full[sa], (ai / kAStages) & 1, abort_flag, status);
+                    if (!ok) break;
+                    if (C.kind == 0)
+                        convert_plane(sm + kOffARaw + sa * kPfPlaneBytes, sm + kOffAF16 + sa * kPfTileBytes, m, C.planes,
+                                      24 - 8 * (C.planes - 1), C.half, ctid, nct);
+                    fence_async_smem();
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(&S.a_conv[sa]);
+                    ++ai;
+                }
+            }
+        }
+    } else {
+        // ---- epilogue: each segment's sums, scaled (2^-ku for low rank,
+        // 2^(dense_exp + E_r - 1037) for dense), added into FP32 registers;
+        // the item's partial y stored in FP64
+        const int q = warp & 3, j = 32 * q + lane;
+        unsigned seg = 0;
+        bool ok = true;
+        for (int it = it0; it < it1 && ok; ++it) {
+            const PfRowItem I = A.row_items[it];
+            float y[kPfMaxRhs];
+#pragma unroll
+            for (int r = 0; r < kPfMaxRhs; ++r) y[r] = 0.0f;
+            const float dexp = ldexpf(1.0f, max(-126, min(127, I.dense_exp)));
+            int c = 0;
+            while (c < I.nchunks) {
+                const int kind = A.chunks[I.chunk0 + c].kind;
+                int c_end = c + 1;
+                while (c_end < I.nchunks && c_end - c < kSegChunks && A.chunks[I.chunk0 + c_end].kind == kind) ++c_end;
+                c = c_end;
+                const int buf = seg & 1;
+                if (!(ok = wait_bar(&S.acc_full[buf], (seg >> 1) & 1, abort_flag, status))) break;
+                ++seg;
+                tc_fence_after();
+                const uint32_t base = tmem + (uint32_t(32 * q) << 16) + uint32_t(buf * kAccStride);
+#pragma unroll
+                for (int g = 0; g < kPfMaxRhs / 16; ++g) {
+                    if (16 * g >= p) break;
+                    float v0[16], v1[16], v2[16];
+                    tmem_ld16(base + 48 * g, v0);
+                    tmem_ld16(base + 48 * g + 16, v1);
+                    tmem_ld16(base + 48 * g + 32, v2);
+                    tmem_wait_ld();
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) {
+                        const int r = 16 * g + i;
+                        const int c0 = 3 * i, c1 = 3 * i + 1, c2 = 3 * i + 2;
+                        const float a0 = c0 < 16 ? v0[c0] : (c0 < 32 ? v1[c0 - 16] : v2[c0 - 32]);
+                        const float a1 = c1 < 16 ? v0[c1] : (c1 < 32 ? v1[c1 - 16] : v2[c1 - 32]);
+                        const float a2 = c2 < 16 ? v0[c2] : (c2 < 32 ? v1[c2 - 16] : v2[c2 - 32]);
+                        const float sc = kind == 0 ? S.flscale[r] : S.fdscale[r] * dexp;
+                        y[r] = fmaf((a0 + a1) + a2, sc, y[r]);
+                    }
+                }
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&S.acc_empty[buf]);
+            }
+            if (!ok) break;
+            if (j < I.rows) {
+                double* out = W.part + ((long long)I.part * kPfM + j) * pu;
+#pragma unroll
+                for (int r = 0; r < kPfMaxRhs; ++r)
+                    if (r < p) out[r] = double(y[r]);
+            }
+        }
+    }
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 1) tmem_free(tmem, 512);
+}
+
+// y[perm[row] * ld + r] = the tile's partials, summed in K-split order.
+__global__ void __launch_bounds__(256) pf_combine_kernel(const int32_t* __restrict__ perm,
+                                                         const int32_t* __restrict__ tile_part0,
+                                                         const double* __restrict__ part, double* __restrict__ y,
+                                                         long long ld, int n, int p, int pu) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)n * p) return;
+    const int row = int(idx / p), r = int(idx % p);
+    const int t = row / kPfM, j = row % kPfM;
+    const int h0 = __ldg(tile_part0 + t), h1 = __ldg(tile_part0 + t + 1);
+    double s = 0.0;
+    for (int h = h0; h < h1; ++h) s += part[((long long)h * kPfM + j) * pu + r];
+    y[(long long)__ldg(perm + row) * ld + r] = s;
+}
+
+}  // namespace pf
+}  // namespace qhg
+
+// ------------------------------------------------------------ host side
+
+using namespace qhg;
+
+struct qh_pmatrix {
+    PfLayout L;
+    int device = 0;
+    int sms = 1;
+    void* arena = nullptr;
+    int32_t* tile_part0 = nullptr;
+    pf::Arena A{};
+    std::mutex mu;
+    void* own_ws = nullptr;
+    size_t own_ws_bytes = 0;
+    ~qh_pmatrix() {
+        int prev = 0;
+        cudaGetDevice(&prev);
+        cudaSetDevice(device);
+        if (arena) cudaFree(arena);
+        if (tile_part0) cudaFree(tile_part0);
+        if (own_ws) cudaFree(own_ws);
+        cudaSetDevice(prev);
+    }
+};
+
+namespace {
+
+struct Guard {
+    int prev = -1;
+    explicit Guard(int dev) {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~Guard() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
+
+int cuda_err(cudaError_t e, const char* what) { return set_error(QH_ECUDA, std::string(what) + ": " + cudaGetErrorString(e)); }
+
+size_t a256(size_t v) { return (v + 255) & ~size_t(255); }
+
+// Scratch layout of one pass of up to 64 right-hand sides.
+struct PfPlan {
+    size_t ex, eu, xt, ut, part, total;
+    int p, pu, N, n_ent;
+};
+
+PfPlan pf_plan(const PfLayout& L, size_t rhs) {
+    PfPlan w{};
+    w.p = int(std::min<size_t>(rhs, kPfMaxRhs));
+    w.pu = (w.p + 15) / 16 * 16;
+    w.N = (3 * w.p + 15) / 16 * 16;
+    w.n_ent = int((L.order + 7) / 8 * 8);
+    size_t off = 0;
+    auto take = [&](size_t b) {
+        const size_t o = off;
+        off += a256(std::max<size_t>(b, 16));
+        return o;
+    };
+    w.ex = take(4 * kPfMaxRhs);
+    w.eu = take(4 * kPfMaxRhs);
+    w.xt = take(2 * size_t(w.N) * size_t(w.n_ent));
+    w.ut = take(4 * size_t(L.n_slots) * size_t(w.pu));
+    w.part = take(8 * size_t(L.n_parts) * kPfM * size_t(w.pu));
+    w.total = off;
+    return w;
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+    });
+    return fn;
+}
+
+int pf_pass(const qh_pmatrix* m, const double* x, double* y, int p, long long ld, void* ws, cudaStream_t s,
+            int* status, void* const* ev) {
+    auto mark = [&](int i) {
+        if (ev) cudaEventRecord(static_cast<cudaEvent_t>(ev[i]), s);
+    };
+    const PfLayout& L = m->L;
+    const PfPlan P = pf_plan(L, size_t(p));
+    auto* w = static_cast<uint8_t*>(ws);
+    pf::Work W;
+    W.ex = reinterpret_cast<int*>(w + P.ex);
+    W.eu = reinterpret_cast<int*>(w + P.eu);
+    W.xt = reinterpret_cast<__half*>(w + P.xt);
+    W.ut = reinterpret_cast<float*>(w + P.ut);
+    W.part = reinterpret_cast<double*>(w + P.part);
+    const int n = int(L.order);
+    auto encode = encode_fn();
+    if (!encode) return set_error(QH_ECUDA, "cuTensorMapEncodeTiled is not available");
+    CUtensorMap map;
+    const cuuint64_t dims[2] = {cuuint64_t(P.n_ent), cuuint64_t(P.N)};
+    const cuuint64_t strides[1] = {cuuint64_t(P.n_ent) * 2};
+    const cuuint32_t box[2] = {cuuint32_t(kPfK), cuuint32_t(P.N)};
+    const cuuint32_t estr[2] = {1, 1};
+    CUresult cr = encode(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, W.xt, dims, strides, box, estr,
+                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (cr != CUDA_SUCCESS) return set_error(QH_ECUDA, "cuTensorMapEncodeTiled failed (" + std::to_string(int(cr)) + ")");
+    cudaError_t e = cudaMemsetAsync(w + P.ex, 0, P.xt - P.ex, s);  // ex, eu
+    if (e != cudaSuccess) return cuda_err(e, "cudaMemsetAsync");
+    mark(0);
+    pf::pf_xmax_kernel<<<(n + 255) / 256, 64, 0, s>>>(x, ld, n, p, W.ex, status);
+    pf::pf_xlimbs_kernel<<<(P.n_ent + 255) / 256, 256, 0, s>>>(x, ld, n, p, P.n_ent, P.N, m->A.perm, W.ex, W.xt);
+    mark(1);
+    if (L.n_col_items > 0)
+        pf::pf_column_kernel<<<L.grid, pf::kThreads, pf::kSmemColumn, s>>>(m->A, W, map, p, P.N, P.pu, status);
+    mark(2);
+    pf::pf_row_kernel<<<L.grid, pf::kThreads, pf::kSmemRow, s>>>(m->A, W, map, p, P.N, P.pu, status);
+    mark(3);
+    const long long total = (long long)n * p;
+    pf::pf_combine_kernel<<<unsigned((total + 255) / 256), 256, 0, s>>>(m->A.perm, m->tile_part0, W.part, y, ld, n,
+                                                                         p, P.pu);
+    mark(4);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_err(e, "CUDA kernel launch");
+    return QH_OK;
+}
+
+template <class F>
+int guarded_pf(F&& f) {
+    try {
+        return f();
+    } catch (const std::invalid_argument& e) {
+        return set_error(QH_EINVAL, e.what());
+    } catch (const std::overflow_error& e) {
+        return set_error(QH_EOVERFLOW, e.what());
+    } catch (const std::bad_alloc&) {
+        return set_error(QH_ERUNTIME, "out of host memory");
+    } catch (const std::exception& e) {
+        return set_error(QH_ERUNTIME, e.what());
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int qh_pmatrix_from_qhmat(const void* bytes, size_t len, int device, qh_pmatrix** out) {
+    if (!out) return set_error(QH_EINVAL, "output handle pointer is null");
+    *out = nullptr;
+    if (!bytes && len) return set_error(QH_EINVAL, "image pointer is null");
+    return guarded_pf([&] {
+        int count = 0;
+        cudaError_t e = cudaGetDeviceCount(&count);
+        if (e != cudaSuccess) return cuda_err(e, "cudaGetDeviceCount");
+        if (!count) return set_error(QH_ERUNTIME, "no CUDA device is available");
+        if (device < 0 || device >= count) return set_error(QH_EINVAL, "invalid CUDA device ordinal");
+        HostMatrix hm = parse_qhmat(static_cast<const uint8_t*>(bytes), len);
+        Guard g(device);
+        int sms = 1, cc_major = 0, cc_minor = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+        cudaDeviceGetAttribute(&cc_major, cudaDevAttrComputeCapabilityMajor, device);
+        cudaDeviceGetAttribute(&cc_minor, cudaDevAttrComputeCapabilityMinor, device);
+        if (cc_major != 10 || cc_minor != 3)
+            return set_error(QH_ERUNTIME, "the precision form needs an sm_103 (GB300) device");
+        auto* m = new (std::nothrow) qh_pmatrix();
+        if (!m) return set_error(QH_ERUNTIME, "out of host memory");
+        m->device = device;
+        m->sms = sms;
+        m->L = build_pf_layout(hm, sms);
+        e = cudaMalloc(&m->arena, m->L.sec.total);
+        if (e == cudaSuccess) e = cudaMemcpy(m->arena, m->L.arena.data(), m->L.sec.total, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMalloc(&m->tile_part0, 4 * m->L.tile_part0.size());
+        if (e == cudaSuccess)
+            e = cudaMemcpy(m->tile_part0, m->L.tile_part0.data(), 4 * m->L.tile_part0.size(), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(pf::pf_column_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, pf::kSmemColumn);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(pf::pf_row_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, pf::kSmemRow);
+        if (e != cudaSuccess) {
+            delete m;
+            return cuda_err(e, "precision form upload");
+        }
+        std::vector<uint8_t>().swap(m->L.arena);
+        const PfSections& S = m->L.sec;
+        auto* b = static_cast<const uint8_t*>(m->arena);
+        m->A.perm = reinterpret_cast<const int32_t*>(b + S.perm);
+        m->A.col_items = reinterpret_cast<const PfColItem*>(b + S.col_items);
+        m->A.comps = reinterpret_cast<const PfComp*>(b + S.comps);
+        m->A.dests = reinterpret_cast<const int32_t*>(b + S.dests);
+        m->A.row_items = reinterpret_cast<const PfRowItem*>(b + S.row_items);
+        m->A.chunks = reinterpret_cast<const PfRowChunk*>(b + S.chunks);
+        m->A.col_sched = reinterpret_cast<const int32_t*>(b + S.col_sched);
+        m->A.row_sched = reinterpret_cast<const int32_t*>(b + S.row_sched);
+        m->A.qraw = b + S.qraw;
+        m->A.praw = b + S.praw;
+        *out = m;
+        return QH_OK;
+    });
+}
+
+void qh_pmatrix_destroy(qh_pmatrix* m) { delete m; }
+
+size_t qh_pworkspace_bytes(const qh_pmatrix* m, size_t rhs) {
+    return m && rhs ? pf_plan(m->L, rhs).total : 0;
+}
+
+int qh_pmatrix_stats(const qh_pmatrix* m, qh_pstats* out) {
+    if (!m || !out) return set_error(QH_EINVAL, "null argument");
+    const PfLayout& L = m->L;
+    out->order = L.order;
+    out->components = uint64_t(L.n_comp);
+    out->code_bytes = L.code_bytes;
+    out->scale_bytes = L.scale_bytes;
+    out->dense_bytes = L.dense_bytes;
+    out->stored_q_bytes = L.stored_q;
+    out->stored_p_bytes = L.stored_p;
+    out->stored_dense_bytes = L.stored_dense;
+    out->device_bytes = L.sec.total;
+    out->col_items = uint64_t(L.n_col_items);
+    out->row_items = uint64_t(L.n_row_items);
+    out->row_slots = uint64_t(L.n_slots);
+    out->mma_elements = L.mma_col + L.mma_row;
+    out->mma_col_elements = L.mma_col;
+    out->mma_row_elements = L.mma_row;
+    out->launches_per_pass = 4 + (L.n_col_items > 0 ? 1 : 0);
+    return QH_OK;
+}
+
+int qh_pmatmul_device(const qh_pmatrix* m, const double* x, double* y, size_t rhs, void* workspace,
+                      size_t workspace_bytes, void* stream, int* status) {
+    return qh_pmatmul_device_profiled(m, x, y, rhs, workspace, workspace_bytes, stream, status, nullptr);
+}
+
+int qh_pmatmul_device_profiled(const qh_pmatrix* m, const double* x, double* y, size_t rhs, void* workspace,
+                               size_t workspace_bytes, void* stream, int* status, void* const* events5) {
+    if (!m) return set_error(QH_EINVAL, "null matrix handle");
+    if (rhs == 0 || rhs > SIZE_MAX / m->L.order) return set_error(QH_EINVAL, "right-hand-side shape mismatch");
+    if (m->L.order * rhs > size_t(INT32_MAX) * 256) return set_error(QH_EOVERFLOW, "CUDA launch grid too large");
+    if (!x || !y) return set_error(QH_EINVAL, "null right-hand side or result pointer");
+    Guard g(m->device);
+    const size_t need = pf_plan(m->L, rhs).total;
+    void* ws = workspace;
+    auto* mm = const_cast<qh_pmatrix*>(m);
+    std::unique_lock<std::mutex> lock(mm->mu, std::defer_lock);
+    if (ws) {
+        if (workspace_bytes < need) return set_error(QH_EINVAL, "workspace too small");
+        if (reinterpret_cast<uintptr_t>(ws) & 255) return set_error(QH_EINVAL, "workspace must be 256-byte aligned");
+    } else {
+        lock.lock();
+        if (mm->own_ws_bytes < need) {
+            if (mm->own_ws) cudaFree(mm->own_ws);
+            mm->own_ws = nullptr;
+            mm->own_ws_bytes = 0;
+            cudaError_t e = cudaMalloc(&mm->own_ws, need);
+            if (e != cudaSuccess) return cuda_err(e, "cudaMalloc");
+            mm->own_ws_bytes = need;
+        }
+        ws = mm->own_ws;
+    }
+    for (size_t c0 = 0; c0 < rhs; c0 += kPfMaxRhs) {
+        const int p = int(std::min<size_t>(kPfMaxRhs, rhs - c0));
+        const int rc = pf_pass(m, x + c0, y + c0, p, (long long)rhs, ws, static_cast<cudaStream_t>(stream), status,
+                               c0 == 0 ? events5 : nullptr);
+        if (rc) return rc;
+    }
+    return QH_OK;
+}
+
+}  // extern "C"

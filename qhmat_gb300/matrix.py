@@ -21,7 +21,7 @@ from pathlib import Path
 
 import numpy as np
 
-from ._lib import QH_STATUS_NONFINITE, QH_STATUS_TIMEOUT, QhBlockDesc, QhStats, load_library, raise_for
+from ._lib import QH_STATUS_NONFINITE, QH_STATUS_TIMEOUT, QhBlockDesc, QhPStats, QhStats, load_library, raise_for
 
 
 def _torch():
@@ -48,12 +48,26 @@ class HMatrix:
 
     # ------------------------------------------------------------ creation
     @classmethod
-    def from_bytes(cls, data: bytes, *, device: int = 0) -> "HMatrix":
-        """Parse and upload a QHMAT001 image (the reference's file format)."""
+    def from_bytes(cls, data: bytes, *, device: int = 0, precision: bool = False) -> "HMatrix":
+        """Parse and upload a QHMAT001 image (the reference's file format).
+
+        ``precision=True`` also uploads the precision form and calibrates the
+        choice between the two forms (``form_choice``) for ``matmul(...,
+        form="auto")``."""
         lib = load_library()
         out = C.c_void_p()
         raise_for(lib.qh_matrix_from_qhmat(bytes(data), len(data), device, C.byref(out)))
-        return cls(out.value, device)
+        h = cls(out.value, device)
+        if precision:
+            h.attach_precision(PrecisionHMatrix.from_bytes(data, device=device))
+        return h
+
+    def attach_precision(self, pf: "PrecisionHMatrix", **calibration) -> dict:
+        """Attach a precision-form handle of the same matrix and calibrate the
+        form used by ``matmul(..., form="auto")`` for two or more columns."""
+        self._pf = pf
+        self.form_choice = choose_form(self, pf, **calibration)
+        return self.form_choice
 
     @classmethod
     def load(cls, path: str | os.PathLike[str], *, device: int = 0) -> "HMatrix":
@@ -143,18 +157,32 @@ class HMatrix:
             raise ValueError("right-hand side has the wrong row count")
         return 1 if len(shape) == 1 else int(shape[1])
 
-    def matmul(self, x, *, device: str = "cuda", stream=None, workspace=None, check: bool = True):
+    def matmul(self, x, *, device: str = "cuda", stream=None, workspace=None, check: bool = True,
+               form: str = "plain"):
         """Apply to an ``(n,)`` vector or ``(n, p)`` array in FP64 on the GPU.
 
         NumPy input returns a new NumPy array; a CUDA float64 torch tensor
         returns a CUDA tensor computed on ``stream`` (default: torch's current
         stream).  ``check=False`` skips the device-side nonfinite check's host
-        synchronisation on the tensor path.
+        synchronisation on the tensor path.  ``form``: "plain" (default; the
+        reference's result to ~1e-15), "precision" (the attached precision
+        form), or "auto" (the precision form for two or more columns when the
+        calibration chose it, else plain).
         """
         if device not in ("cpu", "cuda"):
             raise ValueError("device must be 'cpu' or 'cuda'")
         if device != "cuda":
             raise ValueError("qhmat_gb300 applies on the GPU only; use device='cuda'")
+        if form not in ("plain", "precision", "auto"):
+            raise ValueError("form must be 'plain', 'precision' or 'auto'")
+        if form != "plain":
+            pf = getattr(self, "_pf", None)
+            if pf is None:
+                raise ValueError("no precision form attached (create with precision=True)")
+            shape = tuple(x.shape) if hasattr(x, "shape") else np.shape(x)
+            rhs = 1 if len(shape) == 1 else int(shape[1])
+            if form == "precision" or (rhs >= 2 and self.form_choice["form"] == "precision"):
+                return pf.matmul(x, stream=stream, check=check)
         if _is_torch_tensor(x):
             return self._matmul_tensor(x, stream=stream, workspace=workspace, check=check)
         a = np.ascontiguousarray(np.asarray(x, dtype=np.float64))
@@ -223,6 +251,125 @@ class NativeHMatrix(HMatrix):
         """``NativeHMatrix.reconstruct()`` (src/qhmat/bindings.cpp:180-190): the
         dense matrix, flattened row-major."""
         return self.to_dense().reshape(-1)
+
+
+class PrecisionHMatrix:
+    """The precision form of a resident quantized H-matrix: many right-hand
+    sides per pass over the codes on the tcgen05 tensor cores (f16 digit
+    planes x hi/mid/lo f16 limbs, FP32 accumulation, FP64 scales, dense
+    diagonal limbs and final sums).  Same apply contract as
+    ``HMatrix.matmul``; results carry FP32-level rounding, so callers check
+    them with :func:`precision_gate` against the plain form where they need a
+    stated bound."""
+
+    def __init__(self, handle: int, device: int):
+        self._lib = load_library()
+        self._h = C.c_void_p(handle)
+        self._device = device
+        st = QhPStats()
+        raise_for(self._lib.qh_pmatrix_stats(self._h, C.byref(st)))
+        self._stats = {name: int(getattr(st, name)) for name, _ in QhPStats._fields_}
+
+    @classmethod
+    def from_bytes(cls, data: bytes, *, device: int = 0) -> "PrecisionHMatrix":
+        lib = load_library()
+        out = C.c_void_p()
+        raise_for(lib.qh_pmatrix_from_qhmat(bytes(data), len(data), device, C.byref(out)))
+        return cls(out.value, device)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and self._h.value:
+            self._lib.qh_pmatrix_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001 - interpreter shutdown
+            pass
+
+    @property
+    def order(self) -> int:
+        return self._stats["order"]
+
+    @property
+    def stats(self) -> dict:
+        return dict(self._stats)
+
+    def workspace_bytes(self, rhs: int) -> int:
+        return int(self._lib.qh_pworkspace_bytes(self._h, rhs))
+
+    def matmul(self, x, *, stream=None, workspace=None, check: bool = True):
+        """Apply to ``(n,)`` or ``(n, p)`` FP64 input (NumPy: copied to the
+        device and back; CUDA torch tensor: on ``stream``, result a tensor)."""
+        torch = _torch()
+        numpy_in = not _is_torch_tensor(x)
+        if numpy_in:
+            a = np.ascontiguousarray(np.asarray(x, dtype=np.float64))
+            xt = torch.from_numpy(a).to(torch.device("cuda", self._device))
+        else:
+            xt = x
+            if not xt.is_cuda or xt.device.index != self._device:
+                raise ValueError(f"tensor right-hand side must live on cuda:{self._device}")
+            if xt.dtype != torch.float64:
+                raise ValueError("tensor right-hand side must be torch.float64")
+        shape = tuple(xt.shape)
+        if len(shape) not in (1, 2):
+            raise ValueError("right-hand side must be one- or two-dimensional")
+        if shape[0] != self.order:
+            raise ValueError("right-hand side has the wrong row count")
+        rhs = 1 if len(shape) == 1 else int(shape[1])
+        xt = xt.contiguous()
+        y = torch.empty_like(xt)
+        need = self.workspace_bytes(rhs)
+        if workspace is None:
+            workspace = torch.empty(need, dtype=torch.uint8, device=xt.device)
+        elif workspace.numel() * workspace.element_size() < need:
+            raise ValueError("workspace too small")
+        status = torch.zeros(1, dtype=torch.int32, device=xt.device)
+        s = stream if stream is not None else torch.cuda.current_stream(xt.device)
+        raise_for(self._lib.qh_pmatmul_device(self._h, xt.data_ptr(), y.data_ptr(), rhs, workspace.data_ptr(),
+                                              need, s.cuda_stream, status.data_ptr()))
+        if check or numpy_in:
+            st = int(status.item())
+            if st & QH_STATUS_NONFINITE:
+                raise ValueError("nonfinite right-hand side")
+            if st & QH_STATUS_TIMEOUT:
+                raise RuntimeError("device copy wait timed out")
+        return y.cpu().numpy() if numpy_in else y
+
+
+def precision_gate(y_form, y_plain, x, bound: float) -> dict:
+    """The precision form's acceptance test against the plain form, per
+    right-hand-side column: max_i |y_form - y_plain| <= 0.01 * bound * ||x||_1
+    (the matrix's max-norm reconstruction bound scaled by the column's l1
+    norm, the unit-consistent reading of "1% of reconstruction_bound").
+    Returns the worst column's ratio (pass: <= 1) and both error figures."""
+    yf = np.asarray(y_form, np.float64)
+    yp = np.asarray(y_plain, np.float64)
+    xx = np.asarray(x, np.float64)
+    if yf.ndim == 1:
+        yf, yp, xx = yf[:, None], yp[:, None], xx[:, None]
+    dev = np.max(np.abs(yf - yp), axis=0)
+    limit = 0.01 * bound * np.sum(np.abs(xx), axis=0)
+    ratio = np.where(limit > 0, dev / np.where(limit > 0, limit, 1.0), np.where(dev > 0, np.inf, 0.0))
+    return {"max_abs_dev": float(dev.max()), "worst_ratio": float(ratio.max()),
+            "rel_err": float(np.linalg.norm(yf - yp) / max(np.linalg.norm(yp), 1e-300)),
+            "passes": bool(ratio.max() <= 1.0)}
+
+
+def choose_form(plain: "HMatrix", pf: PrecisionHMatrix, *, probes: int = 8, margin: float = 0.25,
+                seed: int = 20240611) -> dict:
+    """Pick the form for multi-right-hand-side applies of one matrix: apply both
+    forms to ``probes`` seeded N(0, 1) columns and choose the precision form
+    when the worst column's gate ratio (see :func:`precision_gate`) is at most
+    ``margin`` -- a calibration, since the FP32 rounding of the precision
+    form scales with the data and the gate with the matrix's bound."""
+    x = np.random.default_rng(seed).standard_normal((plain.order, probes))
+    gate = precision_gate(pf.matmul(x), plain.matmul(x), x, plain.reconstruction_bound)
+    gate["form"] = "precision" if gate["worst_ratio"] <= margin else "plain"
+    gate["margin"] = margin
+    return gate
 
 
 def cuda_built() -> bool:

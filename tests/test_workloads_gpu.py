@@ -55,10 +55,10 @@ def _check(data, x, threads):
 
 
 def test_split_column_tasks_n4096(cuda_device):
-    """n = 4096 points in the unit square, -log(r + 1e-3), leaf 64: blocks up to
+    """n = 4096 uniform points on [0, 1], -log(r + 1e-3), leaf 64: blocks up to
     1024 columns, so column tasks of 32 chunks run as two parts."""
-    data, rng = _build(4096, 2, 11, "log", 1e-6, 64)
-    assert _widest_block(O.OracleMatrix(data)) > 512
+    data, rng = _build(4096, 1, 11, "log", 1e-6, 64)
+    assert _widest_block(O.OracleMatrix(data)) == 1024
     x = rng.standard_normal(4096)
     _check(data, x, _workers())
     x3 = rng.standard_normal((4096, 3))
