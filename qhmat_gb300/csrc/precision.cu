@@ -70,7 +70,7 @@ constexpr int kWaitLimit = 1 << 22;
 // proportional to the chain length); segments of a few chunks are drained
 // into round-to-nearest FP32 registers by the epilogue warps, from two
 // alternating tensor-memory buffers (columns 0 and 256).
-constexpr int kSegChunks = 4;
+constexpr int kSegChunks = 2;
 constexpr int kAccStride = 256;
 constexpr int kStatusNonfinite = QH_STATUS_NONFINITE;
 constexpr int kStatusTimeout = QH_STATUS_TIMEOUT;

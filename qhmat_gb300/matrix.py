@@ -358,7 +358,7 @@ def precision_gate(y_form, y_plain, x, bound: float) -> dict:
             "passes": bool(ratio.max() <= 1.0)}
 
 
-def choose_form(plain: "HMatrix", pf: PrecisionHMatrix, *, probes: int = 8, margin: float = 0.25,
+def choose_form(plain: "HMatrix", pf: PrecisionHMatrix, *, probes: int = 8, margin: float = 0.5,
                 seed: int = 20240611) -> dict:
     """Pick the form for multi-right-hand-side applies of one matrix: apply both
     forms to ``probes`` seeded N(0, 1) columns and choose the precision form
