@@ -318,6 +318,7 @@ PfLayout build_pf_layout(const HostMatrix& m, int grid) {
     std::vector<PfComp> pcomps;
     std::vector<int32_t> dests;
     std::vector<uint8_t> qraw;
+    double ubound = 0.0;
     for (auto& kv : groups) {
         const int64_t col0 = int64_t(kv.first.first), nn = int64_t(kv.first.second);
         auto& list = kv.second;
@@ -341,8 +342,10 @@ PfLayout build_pf_layout(const HostMatrix& m, int grid) {
                 const Comp& c = comps[size_t(ci)];
                 const size_t g = gcomp(c);
                 const uint32_t* run = m.right_words.data() + m.right_off[g];
+                double l1 = 0.0;  // ||c^Q_j||_1
                 for (int64_t e = 0; e < nn; ++e) {
                     const int32_t code = pf_code(run, uint64_t(e), c.w);
+                    l1 += std::fabs(double(code));
                     const int64_t col = shift + e, kc = col / kPfK, cc = col % kPfK;
                     for (int mm = 0; mm < P; ++mm)
                         base[(size_t(kc) * size_t(P) + size_t(mm)) * kPfPlaneBytes + size_t(j) * kPfK + size_t(cc)] =
@@ -350,6 +353,12 @@ PfLayout build_pf_layout(const HostMatrix& m, int grid) {
                 }
                 PfComp pc{};
                 pc.scale = m.left_scale[g] * m.right_scale[g];
+                // |u_j| <= |s^P s^Q| ||c^Q_j||_1 max|x|; the row side scales u by
+                // 256^(P-1) of its chunk: track the largest such bound
+                int pdmax = 1;
+                for (int32_t dw : comp_dests[size_t(ci)]) pdmax = std::max(pdmax, (dw >> 28) + 1);
+                const double ub = std::fabs(pc.scale) * l1 * std::ldexp(1.0, 8 * (pdmax - 1));
+                if (ub > 0.0 && std::isfinite(ub)) ubound = std::max(ubound, ub);
                 pc.dest0 = int32_t(dests.size());
                 pc.ndest = int32_t(comp_dests[size_t(ci)].size());
                 dests.insert(dests.end(), comp_dests[size_t(ci)].begin(), comp_dests[size_t(ci)].end());
@@ -362,6 +371,9 @@ PfLayout build_pf_layout(const HostMatrix& m, int grid) {
         }
     }
     if (int64_t(qraw.size()) >= (int64_t(1) << 40)) throw std::overflow_error("precision layout too large");
+    // 2^u_beta > every |u_j| 256^(P-1) / max|x| (with a factor 2 of room for
+    // the FP32 rounding of u)
+    L.u_beta = ubound > 0.0 ? std::ilogb(ubound) + 2 : 0;
     L.n_col_items = int32_t(col_items.size());
     L.n_row_items = int32_t(row_items.size());
     L.n_dests = int32_t(dests.size());

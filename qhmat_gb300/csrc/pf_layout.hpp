@@ -95,6 +95,10 @@ struct PfLayout {
     int32_t n_col_items = 0, n_comp = 0, n_dests = 0, n_row_items = 0, n_chunks = 0, n_tiles = 0;
     int32_t n_parts = 0, n_slots = 0;
     int32_t grid = 0;  // persistent CTAs the schedules are built for
+    // Layout-time bound on the row side's u operand: for every component j and
+    // every destination chunk of P planes, |u_j| 256^(P-1) < 2^u_beta max|x|,
+    // so the per-column scale of U' needs no pass over u.
+    int32_t u_beta = 0;
     double bound = 0;
     std::vector<uint8_t> arena;
     PfSections sec{};

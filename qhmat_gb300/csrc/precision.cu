@@ -98,7 +98,6 @@ struct Arena {
 
 struct Work {
     int* ex;       // [64] exponent field of max |x| per right-hand side
-    int* eu;       // [64] exponent field of max |u| per right-hand side
     __half* xt;    // [N][n_ent] f16 limbs of x' (row 3r + l)
     float* ut;     // [n_slots][pu] u per row-side slot
     double* part;  // [n_parts][128][pu] FP64 partial sums of the row side
@@ -245,22 +244,29 @@ __device__ __forceinline__ uint4 digits_to_f16(uint2 w, uint32_t eb, uint32_t su
 // uses ebias = 0 (plane m at 2^(8m-24)), the row side 24 - 8(P-1) (top plane at
 // 2^0).  half 0: 128 stored rows; half 1: stored rows are tile rows 0..63
 // (64..127 zero); half 2: stored rows are tile rows 64..127 (0..63 zero).
+// NT threads (a compile-time count, so that the loop unrolls and each thread
+// keeps several independent loads and conversions in flight).
+template <int NT>
 __device__ __forceinline__ void convert_plane(const uint8_t* raw, uint8_t* tile, int m, int P, int ebias, int half,
-                                              int ctid, int nthreads) {
+                                              int ctid) {
     const uint32_t E = uint32_t(8 * m + 1 + ebias);
     const uint32_t eb = (E << 2) * 0x01010101u;
     const bool top = m == P - 1;
     const uint32_t sub = ((E << 10) | (top ? 0x80u : 0u)) * 0x00010001u;
-    for (int idx = ctid; idx < 1024; idx += nthreads) {
-        const int r = idx >> 3, c = idx & 7;
-        uint4 v;
+    constexpr int kIters = (1024 + NT - 1) / NT;
+    uint2 w[kIters];
+#pragma unroll
+    for (int i = 0; i < kIters; ++i) {
+        const int idx = ctid + i * NT, r = idx >> 3, c = idx & 7;
         const int sr = half == 0 ? r : (half == 1 ? (r < 64 ? r : -1) : (r >= 64 ? r - 64 : -1));
-        if (sr >= 0) {
-            const uint2 w = *reinterpret_cast<const uint2*>(raw + sr * 64 + c * 8);
-            v = digits_to_f16(w, eb, sub, top);
-        } else {
-            v = make_uint4(0u, 0u, 0u, 0u);
-        }
+        w[i] = (idx < 1024 && sr >= 0) ? *reinterpret_cast<const uint2*>(raw + sr * 64 + c * 8) : make_uint2(0u, 0u);
+    }
+#pragma unroll
+    for (int i = 0; i < kIters; ++i) {
+        const int idx = ctid + i * NT, r = idx >> 3, c = idx & 7;
+        if (idx >= 1024) break;
+        const int sr = half == 0 ? r : (half == 1 ? (r < 64 ? r : -1) : (r >= 64 ? r - 64 : -1));
+        const uint4 v = sr >= 0 ? digits_to_f16(w[i], eb, sub, top) : make_uint4(0u, 0u, 0u, 0u);
         *reinterpret_cast<uint4*>(tile + swz_chunk(r, c)) = v;
     }
 }
@@ -271,38 +277,42 @@ __device__ __forceinline__ uint32_t pack_h2(__half a, __half b) {
 
 // U of 64 slots (FP32, row stride pu) -> the f16 B tile: row 3r + l holds limb
 // l of u' = u 2^k[r] 256^(P-1) for the 64 slots of a chunk with P planes
-// (slots >= nvalid: 0).
+// (slots >= nvalid: 0).  Pairs of slots are split with packed conversions.
+template <int NT>
 __device__ __forceinline__ void convert_u(const float* raw, uint8_t* tile, int p, int pu, int nvalid, int P,
-                                          const float* scale, int ctid, int nthreads) {
+                                          const float* scale, int ctid) {
     const float pw = __int_as_float((127 + 8 * (P - 1)) << 23);  // 256^(P-1)
-    for (int idx = ctid; idx < p * 8; idx += nthreads) {
+    constexpr int kIters = (8 * kPfMaxRhs + NT - 1) / NT;
+#pragma unroll
+    for (int it = 0; it < kIters; ++it) {
+        const int idx = ctid + it * NT;
+        if (idx >= p * 8) break;
         const int r = idx % p, kg = idx / p;
         const float sc = scale[r] * pw;
+        float v[8];
+#pragma unroll
+        for (int s = 0; s < 8; ++s) {
+            const int k = 8 * kg + s;
+            v[s] = k < nvalid ? raw[k * pu + r] * sc : 0.0f;
+        }
         uint32_t h[3][4];
 #pragma unroll
         for (int s = 0; s < 8; s += 2) {
-            __half lm[2][3];
-#pragma unroll
-            for (int q = 0; q < 2; ++q) {
-                const int k = 8 * kg + s + q;
-                const float u = k < nvalid ? raw[k * pu + r] * sc : 0.0f;
-                const __half a = __float2half_rn(u);
-                const float r1 = u - __half2float(a);
-                const __half b = __float2half_rn(r1);
-                const float r2 = r1 - __half2float(b);
-                lm[q][0] = a;
-                lm[q][1] = b;
-                lm[q][2] = __float2half_rn(r2);
-            }
-#pragma unroll
-            for (int l = 0; l < 3; ++l) h[l][s >> 1] = pack_h2(lm[0][l], lm[1][l]);
+            const __half2 a = __floats2half2_rn(v[s], v[s + 1]);
+            const float2 af = __half22float2(a);
+            const float r0 = v[s] - af.x, r1 = v[s + 1] - af.y;
+            const __half2 b = __floats2half2_rn(r0, r1);
+            const float2 bf = __half22float2(b);
+            const __half2 c = __floats2half2_rn(r0 - bf.x, r1 - bf.y);
+            h[0][s >> 1] = *reinterpret_cast<const uint32_t*>(&a);
+            h[1][s >> 1] = *reinterpret_cast<const uint32_t*>(&b);
+            h[2][s >> 1] = *reinterpret_cast<const uint32_t*>(&c);
         }
 #pragma unroll
         for (int l = 0; l < 3; ++l)
             *reinterpret_cast<uint4*>(tile + swz_chunk(3 * r + l, kg)) = make_uint4(h[l][0], h[l][1], h[l][2], h[l][3]);
     }
 }
-
 
 // Shared state of one block.
 struct Shared {
@@ -313,7 +323,6 @@ struct Shared {
     uint32_t tmem;
     int abort_flag;
     int ex[kPfMaxRhs];
-    int eu_max[kPfMaxRhs];  // column kernel: this block's max exponent of u
     int ku[kPfMaxRhs];      // row kernel: U' = u 2^ku
     float uscale[kPfMaxRhs];
     float fxscale[kPfMaxRhs];  // column kernel: 2^(24 + E_r - 1037)
@@ -402,7 +411,6 @@ __global__ void __launch_bounds__(kThreads, 1) pf_column_kernel(Arena A, Work W,
     if (tid < kPfMaxRhs) {
         const int E = tid < p ? W.ex[tid] : 0;
         S.ex[tid] = E;
-        S.eu_max[tid] = 0;
         S.fxscale[tid] = E ? ldexpf(1.0f, max(-126, min(127, 24 + E - 1037))) : 0.0f;
     }
     if (warp == 1) tmem_alloc(&S.tmem, 512);
@@ -493,7 +501,7 @@ __global__ void __launch_bounds__(kThreads, 1) pf_column_kernel(Arena A, Work W,
         }
     } else if (warp < kEpiWarp0) {
         // ---- converters: digit planes -> f16 A tiles
-        const int ctid = tid - kConvWarp0 * 32, nct = kConvWarps * 32;
+        const int ctid = tid - kConvWarp0 * 32;
         unsigned ai = 0;
         bool ok = true;
         for (int it = it0; it < it1 && ok; ++it) {
@@ -503,8 +511,8 @@ __global__ void __launch_bounds__(kThreads, 1) pf_column_kernel(Arena A, Work W,
                     const int sa = ai % kAStages;
                     ok = wait_bar(&S.a_full[sa], (ai / kAStages) & 1, abort_flag, status);
                     if (!ok) break;
-                    convert_plane(sm + kOffARaw + sa * kPfPlaneBytes, sm + kOffAF16 + sa * kPfTileBytes, m, I.planes,
-                                  0, 0, ctid, nct);
+                    convert_plane<kConvWarps * 32>(sm + kOffARaw + sa * kPfPlaneBytes, sm + kOffAF16 + sa * kPfTileBytes,
+                                                   m, I.planes, 0, 0, ctid);
                     fence_async_smem();
                     __syncwarp();
                     if (lane == 0) mbar_arrive(&S.a_conv[sa]);
@@ -556,8 +564,6 @@ __global__ void __launch_bounds__(kThreads, 1) pf_column_kernel(Arena A, Work W,
                 if (lane == 0) mbar_arrive(&S.acc_empty[buf]);
             }
             if (!ok) break;
-            int emax = 0;  // largest shift 8(P-1) over this component's destinations
-            for (int d = 0; d < (j < I.count ? C.ndest : 0); ++d) emax = max(emax, 8 * (__ldg(A.dests + C.dest0 + d) >> 28));
 #pragma unroll
             for (int g = 0; g < kPfMaxRhs / 16; ++g) {
                 if (16 * g >= p) break;
@@ -573,18 +579,10 @@ __global__ void __launch_bounds__(kThreads, 1) pf_column_kernel(Arena A, Work W,
 #pragma unroll
                     for (int k = 0; k < 4; ++k) dst[k] = make_float4(u[4 * k], u[4 * k + 1], u[4 * k + 2], u[4 * k + 3]);
                 }
-                // largest exponent of u 256^(P-1) per column over the warp
-#pragma unroll
-                for (int i = 0; i < 16; ++i) {
-                    const int e = int((__float_as_uint(u[i]) >> 23) & 0xFF);
-                    const int m = __reduce_max_sync(0xFFFFFFFFu, e ? e + emax : 0);
-                    if (lane == 0 && m) atomicMax(&S.eu_max[16 * g + i], m);
-                }
             }
         }
     }
     __syncthreads();
-    if (tid < p && S.eu_max[tid]) atomicMax(W.eu + tid, S.eu_max[tid] + 1023 - 127);
     tc_fence_after();
     if (warp == 1) tmem_free(tmem, 512);
 }
@@ -592,7 +590,7 @@ __global__ void __launch_bounds__(kThreads, 1) pf_column_kernel(Arena A, Work W,
 // ------------------------------------------------------------ row kernel
 
 __global__ void __launch_bounds__(kThreads, 1) pf_row_kernel(Arena A, Work W, const __grid_constant__ CUtensorMap xmap,
-                                                             int p, int N, int pu, int* status) {
+                                                             int p, int N, int pu, int u_beta, int* status) {
     extern __shared__ uint8_t smem_dyn[];
     uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_dyn) + 1023) & ~uintptr_t(1023));
     __shared__ Shared S;
@@ -606,11 +604,12 @@ __global__ void __launch_bounds__(kThreads, 1) pf_row_kernel(Arena A, Work W, co
         const int E = tid < p ? W.ex[tid] : 0;
         S.ex[tid] = E;
         S.fdscale[tid] = E ? ldexpf(1.0f, max(-126, min(127, E - 1037))) : 0.0f;
-        const int eu = tid < p ? W.eu[tid] : 0;
-        const int k = eu ? max(-126, min(127, 1037 - eu)) : 0;
+        // U' = u 256^(P-1) 2^k < 2^15 by the layout-time bound
+        // |u| 256^(P-1) < 2^(u_beta + E - 1022)
+        const int k = E ? max(-126, min(127, 1037 - E - u_beta)) : 0;
         S.ku[tid] = k;
-        S.uscale[tid] = eu ? ldexpf(1.0f, k) : 0.0f;
-        S.flscale[tid] = eu ? ldexpf(1.0f, -k) : 0.0f;
+        S.uscale[tid] = E ? ldexpf(1.0f, k) : 0.0f;
+        S.flscale[tid] = E ? ldexpf(1.0f, -k) : 0.0f;
     }
     // B rows 3p .. N-1 of both f16 B stages stay zero (the converters write
     // only rows < 3p; tensor copies of x write zeros there)
@@ -720,7 +719,7 @@ __global__ void __launch_bounds__(kThreads, 1) pf_row_kernel(Arena A, Work W, co
             for (int i = 0; i < kWaitLimit && !mbar_try(&S.drain, 0); ++i) {}
         }
     } else if (warp < kEpiWarp0) {
-        const int ctid = tid - kConvWarp0 * 32, nct = kConvWarps * 32;
+        const int ctid = tid - kConvWarp0 * 32;
         unsigned ai = 0, bi = 0;
         bool ok = true;
         for (int it = it0; it < it1 && ok; ++it) {
@@ -731,8 +730,9 @@ __global__ void __launch_bounds__(kThreads, 1) pf_row_kernel(Arena A, Work W, co
                 ok = wait_bar(&S.b_full[sb], (bi / kBStages) & 1, abort_flag, status);
                 if (!ok) break;
                 if (C.kind == 0)
-                    convert_u(reinterpret_cast<const float*>(sm + kOffBRaw + sb * kURawBytes),
-                              sm + kOffBF16 + sb * kBTileBytes, p, pu, C.nvalid, C.planes, S.uscale, ctid, nct);
+                    convert_u<kConvWarps * 32>(reinterpret_cast<const float*>(sm + kOffBRaw + sb * kURawBytes),
+                                               sm + kOffBF16 + sb * kBTileBytes, p, pu, C.nvalid, C.planes, S.uscale,
+                                               ctid);
                 fence_async_smem();
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&S.b_conv[sb]);
@@ -743,8 +743,9 @@ __global__ void __launch_bounds__(kThreads, 1) pf_row_kernel(Arena A, Work W, co
                     ok = wait_bar(&S.a_full[sa], (ai / kAStages) & 1, abort_flag, status);
                     if (!ok) break;
                     if (C.kind == 0)
-                        convert_plane(sm + kOffARaw + sa * kPfPlaneBytes, sm + kOffAF16 + sa * kPfTileBytes, m, C.planes,
-                                      24 - 8 * (C.planes - 1), C.half, ctid, nct);
+                        convert_plane<kConvWarps * 32>(sm + kOffARaw + sa * kPfPlaneBytes,
+                                                       sm + kOffAF16 + sa * kPfTileBytes, m, C.planes,
+                                                       24 - 8 * (C.planes - 1), C.half, ctid);
                     fence_async_smem();
                     __syncwarp();
                     if (lane == 0) mbar_arrive(&S.a_conv[sa]);
@@ -875,7 +876,7 @@ size_t a256(size_t v) { return (v + 255) & ~size_t(255); }
 
 // Scratch layout of one pass of up to 64 right-hand sides.
 struct PfPlan {
-    size_t ex, eu, xt, ut, part, total;
+    size_t ex, xt, ut, part, total;
     int p, pu, N, n_ent;
 };
 
@@ -892,7 +893,6 @@ PfPlan pf_plan(const PfLayout& L, size_t rhs) {
         return o;
     };
     w.ex = take(4 * kPfMaxRhs);
-    w.eu = take(4 * kPfMaxRhs);
     w.xt = take(2 * size_t(w.N) * size_t(w.n_ent));
     w.ut = take(4 * size_t(L.n_slots) * size_t(w.pu));
     w.part = take(8 * size_t(L.n_parts) * kPfM * size_t(w.pu));
@@ -924,7 +924,6 @@ int pf_pass(const qh_pmatrix* m, const double* x, double* y, int p, long long ld
     auto* w = static_cast<uint8_t*>(ws);
     pf::Work W;
     W.ex = reinterpret_cast<int*>(w + P.ex);
-    W.eu = reinterpret_cast<int*>(w + P.eu);
     W.xt = reinterpret_cast<__half*>(w + P.xt);
     W.ut = reinterpret_cast<float*>(w + P.ut);
     W.part = reinterpret_cast<double*>(w + P.part);
@@ -940,7 +939,7 @@ int pf_pass(const qh_pmatrix* m, const double* x, double* y, int p, long long ld
                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (cr != CUDA_SUCCESS) return set_error(QH_ECUDA, "cuTensorMapEncodeTiled failed (" + std::to_string(int(cr)) + ")");
-    cudaError_t e = cudaMemsetAsync(w + P.ex, 0, P.xt - P.ex, s);  // ex, eu
+    cudaError_t e = cudaMemsetAsync(w + P.ex, 0, P.xt - P.ex, s);  // ex
     if (e != cudaSuccess) return cuda_err(e, "cudaMemsetAsync");
     mark(0);
     pf::pf_xmax_kernel<<<(n + 255) / 256, 64, 0, s>>>(x, ld, n, p, W.ex, status);
@@ -949,7 +948,7 @@ int pf_pass(const qh_pmatrix* m, const double* x, double* y, int p, long long ld
     if (L.n_col_items > 0)
         pf::pf_column_kernel<<<L.grid, pf::kThreads, pf::kSmemColumn, s>>>(m->A, W, map, p, P.N, P.pu, status);
     mark(2);
-    pf::pf_row_kernel<<<L.grid, pf::kThreads, pf::kSmemRow, s>>>(m->A, W, map, p, P.N, P.pu, status);
+    pf::pf_row_kernel<<<L.grid, pf::kThreads, pf::kSmemRow, s>>>(m->A, W, map, p, P.N, P.pu, L.u_beta, status);
     mark(3);
     const long long total = (long long)n * p;
     pf::pf_combine_kernel<<<unsigned((total + 255) / 256), 256, 0, s>>>(m->A.perm, m->tile_part0, W.part, y, ld, n,
