@@ -41,6 +41,7 @@ import os
 import statistics
 import subprocess
 import sys
+import threading
 import time
 from pathlib import Path
 
@@ -58,6 +59,90 @@ WORKLOADS = {
                       "widths 4/8/12/16/24/32, X 32768x64 N(0,1)"),
 }
 PRECISION_WORKLOADS = {"cfg3"}
+SERVING_WORKLOADS = {"cfg5"}
+BATCHING_WORKLOADS = {"cfg4"}
+WORKLOADS["cfg4"] = dict(n=8192, dim=0, seed=3, kernel="mixed", leaf=0, tol_requested=0.0, tol=0.0, rhs=32,
+                         desc="batching: 256 matrices, n log-uniform in [512, 8192], 1-D or 2-D uniform points, "
+                              "1/(r+0.4) or -log(r+1e-3), tolerance log-uniform in [1e-8, 1e-4] escalated x10^0.25 "
+                              "until feasible, leaf 16/32/64, 1-32 N(0,1) columns each (seed 3)")
+WORKLOADS["cfg5"] = dict(n=32768, dim=0, seed=4, kernel="mixed", leaf=0, tol_requested=0.0, tol=0.0, rhs=16,
+                         desc="serving: 16 resident matrices (4 each of n=1024/4096/16384/32768, 1-D or 2-D uniform "
+                              "points, 1/(r+0.4) or -log(r+1e-3), tolerance log-uniform in [1e-8, 1e-4] escalated "
+                              "x10^0.25 until feasible, leaf 16/32/64; seed 4), uploads at 1/s under a 64 GB budget, "
+                              "Poisson arrivals at 20k requests/s of 1-16 N(0,1) columns")
+
+
+def matrix_specs(count: int, seed: int, n_values=None) -> list:
+    """Seeded matrix specs of the batched and served workloads: n log-uniform
+    in [512, 8192] (or cycling through ``n_values``), 1-D or 2-D uniform
+    points, kernel 1/(r+0.4) or -log(r+1e-3), tolerance log-uniform in
+    [1e-8, 1e-4], leaf 16/32/64, 1..32 right-hand-side columns."""
+    import math
+
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    specs = []
+    for i in range(count):
+        n = int(round(math.exp(rng.uniform(math.log(512), math.log(8192)))))
+        if n_values is not None:
+            n = int(n_values[i % len(n_values)])
+        dim = int(rng.integers(1, 3))
+        kernel = "inverse" if rng.integers(0, 2) == 0 else "log"
+        tol = float(math.exp(rng.uniform(math.log(1e-8), math.log(1e-4))))
+        leaf = int(rng.choice([16, 32, 64]))
+        rhs = int(rng.integers(1, 33))
+        specs.append(dict(n=n, dim=dim, kernel=kernel, tol=tol, leaf=leaf, rhs=rhs, seed=int(rng.integers(1 << 31))))
+    return specs
+
+
+def build_spec(spec: dict, workers: int, checksum=None, svd: str = "exact"):
+    """(QHMAT001 image, effective tolerance, attempts) of one spec, with the
+    deterministic escalation rule (x10^0.25 per InfeasibleError)."""
+    import numpy as np
+
+    from qhmat_gb300 import construct
+
+    pts = np.random.default_rng(spec["seed"]).random((spec["n"], spec["dim"]))
+    img, tol, attempts = construct.from_kernel_escalating(pts, spec["kernel"], tolerance=spec["tol"],
+                                                          leaf_size=spec["leaf"], workers=workers, svd=svd)
+    return construct.to_qhmat_bytes(img, checksum=checksum), tol, attempts
+
+
+def _build_spec_job(args):
+    spec, svd = args
+    from oracle import oracle as O
+
+    return build_spec(spec, 1, checksum=O.fnv1a64, svd=svd)
+
+
+def build_specs(specs: list, workers: int, svd: str = "exact") -> list:
+    """Build many specs: small matrices one per worker process (spawn pool),
+    large ones block-parallel; results in spec order."""
+    import multiprocessing as mp
+
+    small = [i for i, sp in enumerate(specs) if sp["n"] <= 8192]
+    large = [i for i, sp in enumerate(specs) if sp["n"] > 8192]
+    out = [None] * len(specs)
+    if small:
+        env = {k: os.environ.get(k) for k in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS")}
+        for k in env:
+            os.environ[k] = "1"
+        try:
+            with mp.get_context("spawn").Pool(max(1, workers)) as pool:
+                for i, res in zip(small, pool.imap(_build_spec_job, [(specs[i], svd) for i in small])):
+                    out[i] = res
+        finally:
+            for k, v in env.items():
+                if v is None:
+                    os.environ.pop(k, None)
+                else:
+                    os.environ[k] = v
+    from oracle import oracle as O
+
+    for i in large:
+        out[i] = build_spec(specs[i], workers, checksum=O.fnv1a64, svd=svd)
+    return out
 
 
 def make_inputs(name: str, workers: int, checksum=None, with_points: bool = False):
@@ -538,6 +623,306 @@ def run_precision(args):
     return 0
 
 
+def run_batching(args):
+    """The batching form: 256 matrices applied as one CUDA graph launch
+    (block-diagonal persistent kernels, per-matrix form choice, autotuned
+    precision schedule) against one plain launch chain per matrix."""
+    world, rank, local = dist_setup()
+    if rank != 0:
+        return 0
+    import ctypes as C
+
+    import numpy as np
+
+    t0 = time.time()
+    specs = matrix_specs(256, 3)
+    built = build_specs(specs, os.cpu_count() or 1, svd="randomized")
+    build_s = time.time() - t0
+    images = [b[0] for b in built]
+    rhs = [sp["rhs"] for sp in specs]
+
+    import torch
+
+    from qhmat_gb300 import HMatrix, _lib, precision_gate
+    from qhmat_gb300.batching import BatchedHMatrices
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    t1 = time.time()
+    bat = BatchedHMatrices(images, rhs, device=local, forms="auto", autotune=True,
+                           cache=os.environ.get("QHMAT_GB300_AUTOTUNE", "/tmp/qhmat_gb300_autotune.json"))
+    setup_s = time.time() - t1
+    rng = np.random.default_rng(3)
+    x_all = torch.from_numpy(rng.standard_normal(bat.total)).to(dev)
+    y_all = torch.zeros_like(x_all)
+    bat.capture(x_all, y_all)
+    s = torch.cuda.current_stream(dev)
+    K, W = args.steps, args.warmup
+    for _ in range(W):
+        bat.replay()
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        clk.wait_first()
+        tl = time.perf_counter()
+        while time.perf_counter() - tl < 0.5:
+            bat.replay()
+            torch.cuda.synchronize(dev)
+        e0.record(s)
+        for _ in range(K):
+            bat.replay()
+        e1.record(s)
+        torch.cuda.synchronize(dev)
+    ms_batch = e0.elapsed_time(e1) / K
+    y_batch = y_all.cpu().numpy()
+
+    # baseline: one plain launch chain per matrix, eager, on one stream
+    lib = _lib.load_library()
+    hs = [HMatrix.from_bytes(img, device=local) for img in images]
+    y_plain = torch.zeros_like(x_all)
+    wss = [torch.empty(max(h.workspace_bytes(r), 256), dtype=torch.uint8, device=dev) for h, r in zip(hs, rhs)]
+    offs = [int(v) for v in bat.x_offsets]
+
+    def per_matrix():
+        for k, h in enumerate(hs):
+            xp = x_all.data_ptr() + 8 * offs[k]
+            yp = y_plain.data_ptr() + 8 * offs[k]
+            _lib.raise_for(lib.qh_matmul_device(h._h, xp, yp, rhs[k], wss[k].data_ptr(), wss[k].numel(),
+                                                s.cuda_stream, None))
+
+    per_matrix()
+    torch.cuda.synchronize(dev)
+    b0, b1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    nb = max(3, K // 4)
+    b0.record(s)
+    for _ in range(nb):
+        per_matrix()
+    b1.record(s)
+    torch.cuda.synchronize(dev)
+    ms_plain = b0.elapsed_time(b1) / nb
+    yp_h = y_plain.cpu().numpy()
+    xh = x_all.cpu().numpy()
+    worst, plain_bitwise = 0.0, True
+    for k in range(len(images)):
+        a, b = offs[k], offs[k + 1]
+        shape = (bat.orders[k], rhs[k])
+        if bat.form[k] == "plain":
+            plain_bitwise &= bool(np.array_equal(y_batch[a:b], yp_h[a:b]))
+        else:
+            g = precision_gate(y_batch[a:b].reshape(shape), yp_h[a:b].reshape(shape), xh[a:b].reshape(shape),
+                               bat.bounds[k])
+            worst = max(worst, g["worst_ratio"])
+    total_rhs = int(sum(rhs))
+    out = {
+        "metric": "batched H-matvec RHS/s (256 matrices, one graph launch)",
+        "value": round(total_rhs / (ms_batch * 1e-3), 1), "unit": "RHS/s", "n_gpus": 1, "steps": K, "warmup": W,
+        "ms_per_step": round(ms_batch, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "per matrix: f64 plain form or f16-limb precision form (calibrated)",
+        "data": "synthetic (seeded points and right-hand sides; matrices constructed on the host)",
+        "config": {"workload": f"cfg4: {WORKLOADS['cfg4']['desc']}", "construction_s": round(build_s, 1),
+                   "construction": "randomized SVD for blocks wider than 128 (seeded; same residual checks)",
+                   "effective_tolerances": [b[1] for b in built], "escalations": [b[2] for b in built]},
+        "forms": {"precision": bat.form.count("precision"), "plain": bat.form.count("plain")},
+        "autotune": bat.tuning, "setup_s": round(setup_s, 1),
+        "per_matrix_plain": {"ms_per_batch": round(ms_plain, 4), "rhs_per_s": round(total_rhs / (ms_plain * 1e-3), 1),
+                             "launches": 4 * len(images)},
+        "speedup_vs_per_matrix_plain": round(ms_plain / ms_batch, 2),
+        "parity": {"plain_matrices_bitwise_equal_to_own_apply": plain_bitwise,
+                   "precision_matrices_worst_gate_ratio": worst},
+        "gpu_launches": "one CUDA graph per step",
+        "clocks": clk.summary(),
+        "e2e": {"value": None, "unit": "RHS/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0,
+                "note": "device-resident packed x and y (graph replay)"},
+    }
+    print(json.dumps(out), flush=True)
+    for h in hs:
+        h.close()
+    bat.close()
+    return 0
+
+
+def run_serving(args):
+    """The serving form under Poisson load (rank 0; the other ranks exit):
+    RHS/s served and p50/p99 request latency of the continuous-batching loop,
+    beside the plain per-request kernel on the same arrival schedule."""
+    world, rank, local = dist_setup()
+    if rank != 0:
+        return 0
+    import numpy as np
+
+    t0 = time.time()
+    workers = os.cpu_count() or 1
+    specs = matrix_specs(16, 4, n_values=(1024, 4096, 16384, 32768))
+    uploads = matrix_specs(4, 40, n_values=(1024, 4096))
+    built = build_specs(specs + uploads, workers, svd="randomized")
+    build_s = time.time() - t0
+
+    import torch
+
+    from qhmat_gb300 import precision_gate
+    from qhmat_gb300.serving import ServingEngine, ServingPool, latency_summary
+
+    torch.cuda.set_device(local)
+    C_cols = 256
+    pool = ServingPool(device=local, budget_bytes=64 << 30)
+    rng = np.random.default_rng(4)
+    keys = []
+    for i, (data, tol, att) in enumerate(built[:16]):
+        r = pool.admit(f"m{i}", data, columns=C_cols)
+        r.x_host.copy_(torch.from_numpy(rng.standard_normal((r.order, C_cols))))
+        keys.append(f"m{i}")
+    forms = {k: pool.get(k).form for k in keys}
+    T = float(os.environ.get("QHMAT_GB300_SERVE_SECONDS", "2.0"))
+    sys.setswitchinterval(2e-4)  # the serving thread and the load generator share the interpreter
+    engine = ServingEngine(pool, streams=4, depth=2, max_cols=64, max_order=32768).start()
+    dev = torch.device("cuda", local)
+    from qhmat_gb300 import _lib as L
+
+    lib = L.load_library()
+    xb = torch.empty(32768 * 16, dtype=torch.float64, device=dev)
+    yb = torch.empty_like(xb)
+    colsb = torch.zeros(16, dtype=torch.int32).pin_memory()
+    wsb = {}
+
+    def schedule(rate, seed):
+        g = np.random.default_rng(seed)
+        n_req = int(rate * T * 1.2) + 16
+        times = np.cumsum(g.exponential(1.0 / rate, n_req))
+        times = times[times < T]
+        return times, g.integers(0, len(keys), times.size), g.integers(1, 17, times.size)
+
+    def col_alloc():
+        ring = {k: 0 for k in keys}
+
+        def col_for(key, k):
+            c = ring[key]
+            if c + k > C_cols:
+                c = 0
+            ring[key] = c + k
+            return c
+        return col_for
+
+    def served_phase(rate, seed):
+        times, req_keys, req_k = schedule(rate, seed)
+        col_for = col_alloc()
+        reqs = []
+        b0, bt0 = engine.batches, engine.batch_cols
+        start = time.perf_counter()
+        i, n = 0, times.size
+        while i < n:
+            # submit every request whose arrival time has come, stamped with
+            # its scheduled arrival; sleep (releasing the interpreter lock to
+            # the serving thread) until the next one
+            now = time.perf_counter() - start
+            while i < n and times[i] <= now:
+                key = keys[int(req_keys[i])]
+                k = int(req_k[i])
+                reqs.append(engine.submit(key, col_for(key, k), k, t_arrival=start + float(times[i])))
+                i += 1
+            if i < n:
+                time.sleep(max(0.0, min(1e-4, times[i] - (time.perf_counter() - start))))
+        t_wait = time.perf_counter()
+        while not all(r.done for r in reqs) and time.perf_counter() - t_wait < 120:
+            time.sleep(0.001)
+        lat = latency_summary(reqs)
+        wall = max(r.t_done for r in reqs) - start
+        nb = engine.batches - b0
+        return reqs, {"offered_requests_per_s": rate, "requests": len(reqs), **lat,
+                      "rhs_per_s": round(lat.get("rhs", 0) / wall, 1), "wall_s": round(wall, 3),
+                      "batches": nb, "mean_batch_columns": round((engine.batch_cols - bt0) / max(1, nb), 2)}
+
+    def plain_phase(rate, seed, limit):
+        """One plain apply per request, in arrival order, on one stream."""
+        times, req_keys, req_k = schedule(rate, seed)
+        col_for = col_alloc()
+        st = torch.cuda.current_stream(dev)
+        lat, rhs_done = [], 0
+        n = min(limit, times.size)
+        start = time.perf_counter()
+        for i in range(n):
+            t_arr, key, k = times[i], keys[int(req_keys[i])], int(req_k[i])
+            while time.perf_counter() - start < t_arr:
+                pass
+            r = pool.get(key)
+            c0 = col_for(key, k)
+            colsb.numpy()[:k] = np.arange(c0, c0 + k, dtype=np.int32)
+            need = r.plain.workspace_bytes(k)
+            if wsb.get(key) is None or wsb[key].numel() < need:
+                wsb[key] = torch.empty(max(need, 1), dtype=torch.uint8, device=dev)
+            L.raise_for(lib.qh_gather_columns(r.x_host.data_ptr(), C_cols, xb.data_ptr(), k, colsb.data_ptr(), k,
+                                              r.order, st.cuda_stream))
+            L.raise_for(lib.qh_matmul_device(r.plain._h, xb.data_ptr(), yb.data_ptr(), k, wsb[key].data_ptr(), need,
+                                             st.cuda_stream, None))
+            torch.cuda.synchronize(dev)
+            lat.append(time.perf_counter() - start - t_arr)
+            rhs_done += k
+        wall = time.perf_counter() - start
+        ll = np.array(lat) * 1e3
+        return {"offered_requests_per_s": rate, "requests": n, "p50_ms": float(np.percentile(ll, 50)),
+                "p99_ms": float(np.percentile(ll, 99)), "rhs_per_s": round(rhs_done / wall, 1),
+                "sample": f"the first {n} requests of the schedule, one plain apply each"}
+
+    stop_uploads = threading.Event()
+    upload_log = []
+
+    def uploader():
+        for j, (data, tol, att) in enumerate(built[16:]):
+            if stop_uploads.wait(1.0):
+                return
+            t = time.perf_counter()
+            try:
+                pool.admit(f"up{j}", data, columns=C_cols)
+                upload_log.append({"key": f"up{j}", "s": round(time.perf_counter() - t, 3), "admitted": True})
+            except Exception as exc:  # noqa: BLE001
+                upload_log.append({"key": f"up{j}", "admitted": False, "error": str(exc)[:120]})
+
+    up = threading.Thread(target=uploader, daemon=True)
+    up.start()
+    reqs, full = served_phase(20000.0, 41)
+    stop_uploads.set()
+    up.join(timeout=30)
+    low_rate = float(os.environ.get("QHMAT_GB300_SERVE_LOW_RATE", "3000"))
+    _, low = served_phase(low_rate, 42)
+    engine.stop(drain=True, timeout=120.0)
+    base_full = plain_phase(20000.0, 41, int(os.environ.get("QHMAT_GB300_SERVE_BASELINE", "4000")))
+    base_low = plain_phase(low_rate, 42, int(low_rate * T))
+    served = full
+    rhs_per_s = full["rhs_per_s"]
+
+    # same y alone as in the mix: recompute some served requests alone
+    worst = 0.0
+    for r in reqs[:: max(1, len(reqs) // 24)][:24]:
+        if not r.done or r.error:
+            continue
+        res = pool.get(r.key)
+        x = res.x_host[:, r.col:r.col + r.k].numpy()
+        y_mix = res.y_host[:, r.col:r.col + r.k].numpy().copy()
+        y_plain = res.plain.matmul(np.ascontiguousarray(x))
+        g = precision_gate(y_mix, y_plain, x, res.plain.reconstruction_bound)
+        worst = max(worst, g["worst_ratio"])
+    rate = 20000.0
+    out = {
+        "metric": "serving RHS/s (continuous batching) and p50/p99 request latency", "value": round(rhs_per_s, 1),
+        "unit": "RHS/s", "n_gpus": 1, "steps": len(reqs), "warmup": 0, "ms_per_step": served.get("mean_ms"),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64 plain / f16-limb precision form per matrix calibration",
+        "data": "synthetic (seeded points and right-hand sides; matrices constructed on the host)",
+        "config": {"workload": f"cfg5: {WORKLOADS['cfg5']['desc']}", "offered_rate": rate, "duration_s": T,
+                   "construction_s": round(build_s, 1),
+                   "matrices": [dict(sp, effective_tol=b[1], attempts=b[2]) for sp, b in zip(specs, built[:16])]},
+        "latency_at_20k": full, "latency_sustained": low,
+        "plain_per_request_at_20k": base_full, "plain_per_request_sustained": base_low,
+        "forms": forms, "hbm_resident_bytes": pool.used_bytes, "uploads": upload_log,
+        "mix_gate_worst_ratio": worst,
+        "e2e": {"value": round(rhs_per_s, 1), "unit": "RHS/s", "h2d_bytes_per_step": None,
+                "d2h_bytes_per_step": None,
+                "transfer": "request columns read from and results written to pinned host memory by the "
+                            "gather/scatter kernels"},
+    }
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -554,6 +939,10 @@ def main():
         return run_reference_arm(args)
     if args.workload in PRECISION_WORKLOADS:
         return run_precision(args)
+    if args.workload in SERVING_WORKLOADS:
+        return run_serving(args)
+    if args.workload in BATCHING_WORKLOADS:
+        return run_batching(args)
 
     world, rank, local = dist_setup()
     import numpy as np

@@ -259,6 +259,63 @@ QH_API int qh_pmatmul_device_profiled(const qh_pmatrix* m, const double* x, doub
                                       void* workspace, size_t workspace_bytes, void* stream, int* status,
                                       void* const* events5);
 
+/* ---- Batched applies (serving): column gather / scatter ----
+ *
+ * The reference applies one request at a time and copies every operand per
+ * call (src/qhmat/bindings.cpp:152-179, src/qhmat/cuda.cu:143-164).  A serving
+ * loop here gathers the columns of many requests into one multi-column
+ * operand, applies once, and scatters the result columns back:
+ *   gather:  dst[i * ld_dst + j] = src[i * ld_src + cols[j]]
+ *   scatter: dst[i * ld_dst + cols[j]] = src[i * ld_src + j]
+ * for rows i < n and j < ncols.  src / dst may be device memory or pinned
+ * host memory the device reads and writes directly; cols is a device (or
+ * pinned host) array of ncols column indices.  Stream-ordered, no copies of
+ * their own.  No reference counterpart. */
+QH_API int qh_gather_columns(const double* src, long long ld_src, double* dst, long long ld_dst,
+                             const int32_t* cols, int ncols, size_t n, void* stream);
+QH_API int qh_scatter_columns(const double* src, long long ld_src, double* dst, long long ld_dst,
+                              const int32_t* cols, int ncols, size_t n, void* stream);
+
+/* ---- Batching form: many matrices in one launch chain ----
+ *
+ * The reference applies one matrix per call.  A batch here is the
+ * block-diagonal matrix diag(A_1, .., A_M) of M QHMAT001 images (offsets[k]
+ * receives matrix k's first row: consecutive for the plain form, each on a
+ * multiple of 128 rows for the precision form), resident as one plain-form
+ * handle (qh_matrix_from_batch) or one
+ * precision-form handle (qh_pmatrix_from_batch, whose persistent schedule uses
+ * `grid` CTAs (0: one per SM) and about `row_items_per_cta` row items per CTA
+ * (0: 3) -- the parameters the batching form's autotuner sets).  One
+ * qh_matmul_device / qh_pmatmul_device call on the handle then walks the
+ * blocks of every matrix in one persistent launch of each kernel.
+ *
+ * Right-hand sides of different sizes are packed: matrix k's x (order_k x
+ * rhs_k, row-major, source order) at x_all + x_offset, its y at y_all +
+ * y_offset.  qh_batch_gather builds the block-diagonal operand xs ((sum of
+ * padded orders) x P, P = the largest rhs_k) with every column of every
+ * matrix scaled by a power of two so that its largest |x| is in [1, 2)
+ * (exps receives the exponents, count x P ints of device scratch), zero in
+ * padding rows and columns; qh_batch_scatter scales the result back into
+ * y_all, exactly.  table: a device array of count entries.  No reference
+ * counterpart. */
+typedef struct {
+    uint64_t offset;   /* first row of the matrix in the block-diagonal operand */
+    uint64_t order;    /* its order */
+    uint64_t rows;     /* rows up to the next matrix (order plus padding) */
+    uint64_t rhs;      /* its right-hand-side columns */
+    uint64_t x_offset; /* element offset of its x in x_all */
+    uint64_t y_offset; /* element offset of its y in y_all */
+} qh_batch_entry;
+
+QH_API int qh_matrix_from_batch(const void* const* images, const size_t* lens, size_t count, int device,
+                                qh_matrix** out, uint64_t* offsets);
+QH_API int qh_pmatrix_from_batch(const void* const* images, const size_t* lens, size_t count, int device, int grid,
+                                 double row_items_per_cta, qh_pmatrix** out, uint64_t* offsets);
+QH_API int qh_batch_gather(const qh_batch_entry* table, size_t count, int P, const double* x_all, double* xs,
+                           int* exps, void* stream);
+QH_API int qh_batch_scatter(const qh_batch_entry* table, size_t count, int P, const double* ys, const int* exps,
+                            double* y_all, void* stream);
+
 /* Test aid for the bounded device waits: one warp on `device` waits at most
  * `polls` (1 .. 2^20) tests on an mbarrier that nothing completes -- no copy
  * is issued -- and records the timeout in a status int exactly as the apply

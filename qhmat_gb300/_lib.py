@@ -96,6 +96,19 @@ def load_library() -> C.CDLL:
     lib.qh_pmatmul_device.argtypes = [vp, vp, vp, sz, vp, sz, vp, vp]
     lib.qh_pmatmul_device_profiled.restype = i32
     lib.qh_pmatmul_device_profiled.argtypes = [vp, vp, vp, sz, vp, sz, vp, vp, vp]
+    ll = C.c_longlong
+    for name in ("qh_gather_columns", "qh_scatter_columns"):
+        f = getattr(lib, name)
+        f.restype = i32
+        f.argtypes = [vp, ll, vp, ll, vp, i32, sz, vp]
+    lib.qh_matrix_from_batch.restype = i32
+    lib.qh_matrix_from_batch.argtypes = [vp, vp, sz, i32, C.POINTER(vp), vp]
+    lib.qh_pmatrix_from_batch.restype = i32
+    lib.qh_pmatrix_from_batch.argtypes = [vp, vp, sz, i32, i32, C.c_double, C.POINTER(vp), vp]
+    lib.qh_batch_gather.restype = i32
+    lib.qh_batch_gather.argtypes = [vp, sz, i32, vp, vp, vp, vp]
+    lib.qh_batch_scatter.restype = i32
+    lib.qh_batch_scatter.argtypes = [vp, sz, i32, vp, vp, vp, vp]
     lib.qh_debug_wait_timeout.restype = i32
     lib.qh_debug_wait_timeout.argtypes = [i32, i32]
     lib.qh_matrix_reconstruct.restype = i32

@@ -50,6 +50,7 @@
 #include <unistd.h>
 
 #include "../../include/qhmat_gb300.h"
+#include "batch.hpp"
 #include "errors.hpp"
 #include "layout.hpp"
 
@@ -1776,6 +1777,29 @@ int qh_matrix_from_arrays(size_t order, const size_t* permutation, size_t block_
         validate(hm);
         Layout L = build_layout(hm);
         return upload(std::move(L), device, out);
+    });
+}
+
+int qh_matrix_from_batch(const void* const* images, const size_t* lens, size_t count, int device, qh_matrix** out,
+                         uint64_t* offsets) {
+    if (!out) return fail(QH_EINVAL, "output handle pointer is null");
+    *out = nullptr;
+    if (!images || !lens || !count) return fail(QH_EINVAL, "empty batch");
+    return guarded([&] {
+        std::vector<HostMatrix> ms;
+        ms.reserve(count);
+        for (size_t k = 0; k < count; ++k) ms.push_back(parse_qhmat(static_cast<const uint8_t*>(images[k]), lens[k]));
+        std::vector<uint64_t> off;
+        // no padding rows: the plain layout's row tiles already stay inside
+        // the row slabs of blocks (so inside one matrix), and every row of
+        // the block-diagonal matrix must belong to some block
+        HostMatrix S = concat_block_diagonal(ms, 1, off);
+        std::vector<HostMatrix>().swap(ms);
+        Layout L = build_layout(S);
+        const int rc = upload(std::move(L), device, out);
+        if (rc == QH_OK && offsets)
+            for (size_t k = 0; k < count; ++k) offsets[k] = off[k];
+        return rc;
     });
 }
 

@@ -98,7 +98,7 @@ size_t align_to(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
 }  // namespace
 
-PfLayout build_pf_layout(const HostMatrix& m, int grid) {
+PfLayout build_pf_layout(const HostMatrix& m, int grid, double row_items_per_cta) {
     PfLayout L;
     L.order = m.order;
     L.bound = m.reconstruction_bound();
@@ -273,8 +273,7 @@ PfLayout build_pf_layout(const HostMatrix& m, int grid) {
     std::vector<double> row_cost;
     {
         const double total = std::accumulate(tile_cost.begin(), tile_cost.end(), 0.0);
-        double per_cta = 3.0;
-        if (const char* v = std::getenv("QHMAT_GB300_PF_ROW_ITEMS")) per_cta = std::max(1.0, std::atof(v));
+        const double per_cta = row_items_per_cta > 0.0 ? std::max(1.0, row_items_per_cta) : 3.0;
         const double target = std::max(1.0, total / (per_cta * L.grid));
         L.tile_part0.assign(size_t(n_tiles) + 1, 0);
         int32_t part = 0;

@@ -110,8 +110,11 @@ struct PfLayout {
     uint64_t mma_col = 0, mma_row = 0;  // M x K elements streamed through the MMAs per pass
 };
 
-// Build the precision-form layout of a validated matrix; `grid` is the number
-// of persistent CTAs whose static schedules are stored with it.
-PfLayout build_pf_layout(const HostMatrix& m, int grid);
+// Build the precision-form layout of a matrix; `grid` is the number of
+// persistent CTAs whose static schedules are stored with it, and
+// `row_items_per_cta` (default 3) how many row items (K splits of the 128-row
+// tiles) each CTA gets on average -- the two schedule parameters the batching
+// form's autotuner chooses.
+PfLayout build_pf_layout(const HostMatrix& m, int grid, double row_items_per_cta = 0.0);
 
 }  // namespace qhg

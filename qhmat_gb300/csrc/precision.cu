@@ -49,6 +49,7 @@
 #include "../../include/qhmat_gb300.h"
 #include "errors.hpp"
 #include "layout.hpp"
+#include "batch.hpp"
 #include "pf_layout.hpp"
 
 namespace qhg {
@@ -974,6 +975,53 @@ int guarded_pf(F&& f) {
     }
 }
 
+// Build the precision layout of a matrix for `device` and upload it.
+int pf_upload(const HostMatrix& hm, int device, int grid, double row_items_per_cta, qh_pmatrix** out) {
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess) return cuda_err(e, "cudaGetDeviceCount");
+    if (!count) return set_error(QH_ERUNTIME, "no CUDA device is available");
+    if (device < 0 || device >= count) return set_error(QH_EINVAL, "invalid CUDA device ordinal");
+    Guard g(device);
+    int sms = 1, cc_major = 0, cc_minor = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    cudaDeviceGetAttribute(&cc_major, cudaDevAttrComputeCapabilityMajor, device);
+    cudaDeviceGetAttribute(&cc_minor, cudaDevAttrComputeCapabilityMinor, device);
+    if (cc_major != 10 || cc_minor != 3) return set_error(QH_ERUNTIME, "the precision form needs an sm_103 (GB300) device");
+    auto* m = new (std::nothrow) qh_pmatrix();
+    if (!m) return set_error(QH_ERUNTIME, "out of host memory");
+    m->device = device;
+    m->sms = sms;
+    m->L = build_pf_layout(hm, grid > 0 ? std::min(grid, sms) : sms, row_items_per_cta);
+    e = cudaMalloc(&m->arena, m->L.sec.total);
+    if (e == cudaSuccess) e = cudaMemcpy(m->arena, m->L.arena.data(), m->L.sec.total, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc(&m->tile_part0, 4 * m->L.tile_part0.size());
+    if (e == cudaSuccess)
+        e = cudaMemcpy(m->tile_part0, m->L.tile_part0.data(), 4 * m->L.tile_part0.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(pf::pf_column_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, pf::kSmemColumn);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(pf::pf_row_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, pf::kSmemRow);
+    if (e != cudaSuccess) {
+        delete m;
+        return cuda_err(e, "precision form upload");
+    }
+    std::vector<uint8_t>().swap(m->L.arena);
+    const PfSections& S = m->L.sec;
+    auto* b = static_cast<const uint8_t*>(m->arena);
+    m->A.perm = reinterpret_cast<const int32_t*>(b + S.perm);
+    m->A.col_items = reinterpret_cast<const PfColItem*>(b + S.col_items);
+    m->A.comps = reinterpret_cast<const PfComp*>(b + S.comps);
+    m->A.dests = reinterpret_cast<const int32_t*>(b + S.dests);
+    m->A.row_items = reinterpret_cast<const PfRowItem*>(b + S.row_items);
+    m->A.chunks = reinterpret_cast<const PfRowChunk*>(b + S.chunks);
+    m->A.col_sched = reinterpret_cast<const int32_t*>(b + S.col_sched);
+    m->A.row_sched = reinterpret_cast<const int32_t*>(b + S.row_sched);
+    m->A.qraw = b + S.qraw;
+    m->A.praw = b + S.praw;
+    *out = m;
+    return QH_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -983,52 +1031,27 @@ int qh_pmatrix_from_qhmat(const void* bytes, size_t len, int device, qh_pmatrix*
     *out = nullptr;
     if (!bytes && len) return set_error(QH_EINVAL, "image pointer is null");
     return guarded_pf([&] {
-        int count = 0;
-        cudaError_t e = cudaGetDeviceCount(&count);
-        if (e != cudaSuccess) return cuda_err(e, "cudaGetDeviceCount");
-        if (!count) return set_error(QH_ERUNTIME, "no CUDA device is available");
-        if (device < 0 || device >= count) return set_error(QH_EINVAL, "invalid CUDA device ordinal");
         HostMatrix hm = parse_qhmat(static_cast<const uint8_t*>(bytes), len);
-        Guard g(device);
-        int sms = 1, cc_major = 0, cc_minor = 0;
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-        cudaDeviceGetAttribute(&cc_major, cudaDevAttrComputeCapabilityMajor, device);
-        cudaDeviceGetAttribute(&cc_minor, cudaDevAttrComputeCapabilityMinor, device);
-        if (cc_major != 10 || cc_minor != 3)
-            return set_error(QH_ERUNTIME, "the precision form needs an sm_103 (GB300) device");
-        auto* m = new (std::nothrow) qh_pmatrix();
-        if (!m) return set_error(QH_ERUNTIME, "out of host memory");
-        m->device = device;
-        m->sms = sms;
-        m->L = build_pf_layout(hm, sms);
-        e = cudaMalloc(&m->arena, m->L.sec.total);
-        if (e == cudaSuccess) e = cudaMemcpy(m->arena, m->L.arena.data(), m->L.sec.total, cudaMemcpyHostToDevice);
-        if (e == cudaSuccess) e = cudaMalloc(&m->tile_part0, 4 * m->L.tile_part0.size());
-        if (e == cudaSuccess)
-            e = cudaMemcpy(m->tile_part0, m->L.tile_part0.data(), 4 * m->L.tile_part0.size(), cudaMemcpyHostToDevice);
-        if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(pf::pf_column_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, pf::kSmemColumn);
-        if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(pf::pf_row_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, pf::kSmemRow);
-        if (e != cudaSuccess) {
-            delete m;
-            return cuda_err(e, "precision form upload");
-        }
-        std::vector<uint8_t>().swap(m->L.arena);
-        const PfSections& S = m->L.sec;
-        auto* b = static_cast<const uint8_t*>(m->arena);
-        m->A.perm = reinterpret_cast<const int32_t*>(b + S.perm);
-        m->A.col_items = reinterpret_cast<const PfColItem*>(b + S.col_items);
-        m->A.comps = reinterpret_cast<const PfComp*>(b + S.comps);
-        m->A.dests = reinterpret_cast<const int32_t*>(b + S.dests);
-        m->A.row_items = reinterpret_cast<const PfRowItem*>(b + S.row_items);
-        m->A.chunks = reinterpret_cast<const PfRowChunk*>(b + S.chunks);
-        m->A.col_sched = reinterpret_cast<const int32_t*>(b + S.col_sched);
-        m->A.row_sched = reinterpret_cast<const int32_t*>(b + S.row_sched);
-        m->A.qraw = b + S.qraw;
-        m->A.praw = b + S.praw;
-        *out = m;
-        return QH_OK;
+        return pf_upload(hm, device, 0, 0.0, out);
+    });
+}
+
+int qh_pmatrix_from_batch(const void* const* images, const size_t* lens, size_t count, int device, int grid,
+                          double row_items_per_cta, qh_pmatrix** out, uint64_t* offsets) {
+    if (!out) return set_error(QH_EINVAL, "output handle pointer is null");
+    *out = nullptr;
+    if (!images || !lens || !count) return set_error(QH_EINVAL, "empty batch");
+    return guarded_pf([&] {
+        std::vector<HostMatrix> ms;
+        ms.reserve(count);
+        for (size_t k = 0; k < count; ++k) ms.push_back(parse_qhmat(static_cast<const uint8_t*>(images[k]), lens[k]));
+        std::vector<uint64_t> off;
+        HostMatrix S = concat_block_diagonal(ms, kPfM, off);
+        std::vector<HostMatrix>().swap(ms);
+        const int rc = pf_upload(S, device, grid, row_items_per_cta, out);
+        if (rc == QH_OK && offsets)
+            for (size_t k = 0; k < count; ++k) offsets[k] = off[k];
+        return rc;
     });
 }
 

@@ -56,3 +56,27 @@ def test_invalid_arguments_raise():
         K.from_kernel(pts, "inverse", tolerance=1e-6, bit_widths=(1, 8))
     with pytest.raises(ValueError):
         K.from_kernel(pts, "nope", tolerance=1e-6)
+
+
+def test_randomized_svd_path_builds_a_valid_matrix():
+    """The fast construction path: every block passes the reference's
+    residual and allocation checks, the matrix applies like the dense kernel
+    matrix within its bound, and it is deterministic."""
+    import numpy as np
+
+    from oracle import oracle as O
+    from qhmat_gb300 import construct
+
+    rng = np.random.default_rng(3)
+    pts = rng.random((2048, 1))
+    img = construct.from_kernel(pts, "log", tolerance=1e-6, leaf_size=32, workers=1, svd="randomized")
+    data = construct.to_qhmat_bytes(img, checksum=O.fnv1a64)
+    again = construct.to_qhmat_bytes(construct.from_kernel(pts, "log", tolerance=1e-6, leaf_size=32, workers=1,
+                                                           svd="randomized"), checksum=O.fnv1a64)
+    assert data == again
+    m = O.OracleMatrix(data)
+    x = rng.standard_normal(2048)
+    a = construct.kernel_matrix(pts, "log")
+    err = np.max(np.abs(m.matmul(x) - a @ x))
+    assert err <= m.reconstruction_bound * np.sum(np.abs(x))
+    assert max(b.rank for b in img.blocks if b.dense is None) <= 96
