@@ -220,14 +220,18 @@ class ServingEngine:
     ``request.done`` turns true, with ``t_done`` set, once its columns of the
     output buffer hold y.  ``cancel(request)`` drops a request that has not
     been dispatched yet.  Batches: up to ``max_cols`` columns of one matrix;
-    ``streams`` x ``depth`` batches in flight."""
+    ``streams`` x ``depth`` batches in flight; batches of plain-form
+    matrices stop at ``plain_max_cols`` columns."""
 
     def __init__(self, pool: ServingPool, *, streams: int = 4, depth: int = 2, max_cols: int = 64,
-                 max_order: int = 1 << 15):
+                 plain_max_cols: int = 16, max_order: int = 1 << 15):
         import torch
 
         self.pool = pool
         self.max_cols = max_cols
+        # the plain form's work grows with the columns it is given, so larger
+        # batches only delay the requests behind them
+        self.plain_max_cols = min(plain_max_cols, max_cols)
         self._lib = load_library()
         self._queue: collections.deque = collections.deque()
         self._pending: "collections.OrderedDict[object, collections.deque]" = collections.OrderedDict()
@@ -363,8 +367,10 @@ class ServingEngine:
                         break
                     _, key = min(live)
                     q = self._pending[key]
+                    res = self.pool.get(key)
+                    cap = self.max_cols if res.form == "precision" else self.plain_max_cols
                     batch, cols = [], 0
-                    while q and cols + q[0].k <= self.max_cols:
+                    while q and (not batch or cols + q[0].k <= cap):
                         r = q.popleft()
                         batch.append(r)
                         cols += r.k
