@@ -111,9 +111,7 @@ def build_spec(spec: dict, workers: int, checksum=None, svd: str = "exact"):
 
 def _build_spec_job(args):
     spec, svd = args
-    from oracle import oracle as O
-
-    return build_spec(spec, 1, checksum=O.fnv1a64, svd=svd)
+    return build_spec(spec, 1, svd=svd)
 
 
 def build_specs(specs: list, workers: int, svd: str = "exact") -> list:
@@ -138,10 +136,8 @@ def build_specs(specs: list, workers: int, svd: str = "exact") -> list:
                     os.environ.pop(k, None)
                 else:
                     os.environ[k] = v
-    from oracle import oracle as O
-
     for i in large:
-        out[i] = build_spec(specs[i], workers, checksum=O.fnv1a64, svd=svd)
+        out[i] = build_spec(specs[i], workers, svd=svd)
     return out
 
 
