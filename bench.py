@@ -548,6 +548,13 @@ def run_precision(args):
     model_bytes = h.model_bytes(rhs)
     model_flops = rhs * h.stats["flops_per_rhs"]
     value = rhs * world / (ms_step * 1e-3)
+    traffic = None
+    traffic_file = ROOT / "profiles" / f"traffic_{args.workload}.json"
+    if traffic_file.exists():
+        try:
+            traffic = json.loads(traffic_file.read_text()).get(dom)
+        except ValueError:
+            traffic = None
     out = {
         "metric": "H-matvec RHS/s (precision form, X 32768x64)", "value": round(value, 1), "unit": "RHS/s",
         "n_gpus": world, "steps": K, "warmup": args.warmup, "ms_per_step": round(ms_step, 5),
@@ -558,7 +565,7 @@ def run_precision(args):
         "roofline": {"bound": bound, "kernel": dom, "achieved": round(achieved, 1),
                      "peak": tc_peak if bound == "tensor" else hbm_peak,
                      "unit": "TFLOP/s" if bound == "tensor" else "GB/s",
-                     "frac": round(max(tfrac, hfrac), 4), "traffic": None,
+                     "frac": round(max(tfrac, hfrac), 4), "traffic": traffic,
                      "tensor_frac": round(tfrac, 4), "hbm_frac": round(hfrac, 4),
                      "kernel_ms": {k: round(v, 5) for k, v in kmean.items()},
                      "mma_flops": kflops, "moved_bytes": kbytes,
