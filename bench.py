@@ -892,6 +892,10 @@ def run_serving(args):
     up.join(timeout=30)
     low_rate = float(os.environ.get("QHMAT_GB300_SERVE_LOW_RATE", "3000"))
     _, low = served_phase(low_rate, 42)
+    # the load curve between the sustained and the offered rate
+    by_rate = {}
+    for j, mid in enumerate((6000.0, 10000.0, 14000.0)):
+        _, by_rate[str(int(mid))] = served_phase(mid, 43 + j)
     engine.stop(drain=True, timeout=120.0)
     base_full = plain_phase(20000.0, 41, float(os.environ.get("QHMAT_GB300_SERVE_BASELINE_S", "20")))
     base_low = plain_phase(low_rate, 42, 60.0)
@@ -919,7 +923,7 @@ def run_serving(args):
         "config": {"workload": f"cfg5: {WORKLOADS['cfg5']['desc']}", "offered_rate": rate, "duration_s": T,
                    "construction_s": round(build_s, 1),
                    "matrices": [dict(sp, effective_tol=b[1], attempts=b[2]) for sp, b in zip(specs, built[:16])]},
-        "latency_at_20k": full, "latency_sustained": low,
+        "latency_at_20k": full, "latency_sustained": low, "latency_by_offered_rate": by_rate,
         "plain_per_request_at_20k": base_full, "plain_per_request_sustained": base_low,
         "forms": forms, "hbm_resident_bytes": pool.used_bytes, "uploads": upload_log,
         "mix_gate_worst_ratio": worst,

@@ -23,7 +23,8 @@
 //                        order (deterministic), scattered through perm.
 //
 // Both streaming kernels are persistent and warp-specialised: one warp issues
-// the bulk and tensor copies into a ring of shared-memory stages, six warps
+// the bulk and tensor copies into a ring of shared-memory stages, six (column)
+// or eight (row) warps
 // turn digit bytes (and U) into f16 operand tiles, one thread issues the
 // MMAs, four warps drain the accumulators from tensor memory.  Every wait is
 // bounded; a wait that gives up sets QH_STATUS_TIMEOUT and the block winds
@@ -55,11 +56,22 @@
 namespace qhg {
 namespace pf {
 
-constexpr int kThreads = 384;     // 12 warps
-constexpr int kConvWarp0 = 2;     // warps 2..7 convert
-constexpr int kConvWarps = 6;
-constexpr int kEpiWarp0 = 8;      // warps 8..11 drain tensor memory (lane quarters 0..3)
-constexpr int kAStages = 4;
+// Warp roles of both kernels: warp 0 issues the copies, one thread of warp 1
+// the MMAs, warps 2 .. 2+C-1 convert, the last four drain tensor memory (lane
+// quarters 0..3).  The row kernel converts U as well as digit planes; it runs
+// eight converters (two per scheduler) and keeps its y sums in tensor memory,
+// which leaves them the registers.  The column kernel runs six.
+template <int CONV, int ASTAGES>
+struct Roles {
+    static constexpr int kConvWarps = CONV;
+    static constexpr int kEpiWarp0 = 2 + CONV;
+    static constexpr int kThreads = 32 * (kEpiWarp0 + 4);
+    static constexpr int kAStages = ASTAGES;  // digit-plane stages (raw and f16)
+};
+using ColRoles = Roles<6, 4>;
+using RowRoles = Roles<8, 5>;
+constexpr int kConvWarp0 = 2;
+constexpr int kMaxAStages = 5;
 constexpr int kBStages = 2;
 constexpr int kNMax = 192;        // N of one pass (3 limbs x 64 right-hand sides)
 constexpr int kBTileBytes = kNMax * 128;   // B operand stage (N rows of 64 f16)
@@ -76,13 +88,20 @@ constexpr int kAccStride = 256;
 constexpr int kStatusNonfinite = QH_STATUS_NONFINITE;
 constexpr int kStatusTimeout = QH_STATUS_TIMEOUT;
 
-// Shared-memory map of both kernels (offsets from a 1024-byte-aligned base).
-constexpr int kOffAF16 = 0;                                    // 4 x 16 KB f16 A tiles
-constexpr int kOffBF16 = kOffAF16 + kAStages * kPfTileBytes;   // 2 x 24 KB f16 B tiles
-constexpr int kOffARaw = kOffBF16 + kBStages * kBTileBytes;    // 4 x 8 KB digit planes
-constexpr int kOffBRaw = kOffARaw + kAStages * kPfPlaneBytes;  // 2 x 16 KB FP32 u (row kernel)
-constexpr int kSmemColumn = kOffBRaw + 1024;                   // + alignment slack
-constexpr int kSmemRow = kOffBRaw + kBStages * kURawBytes + 1024;
+// Shared-memory map (offsets from a 1024-byte-aligned base): the f16 A tiles
+// (16 KB each), the f16 B tiles (24 KB), the raw digit planes (8 KB) and, in
+// the row kernel, the raw FP32 u of a chunk (16 KB).
+template <class R>
+struct SmemMap {
+    static constexpr int kOffAF16 = 0;
+    static constexpr int kOffBF16 = kOffAF16 + R::kAStages * kPfTileBytes;
+    static constexpr int kOffARaw = kOffBF16 + kBStages * kBTileBytes;
+    static constexpr int kOffBRaw = kOffARaw + R::kAStages * kPfPlaneBytes;
+};
+constexpr int kSmemColumn = SmemMap<ColRoles>::kOffBRaw + 1024;  // + alignment slack
+constexpr int kSmemRow = SmemMap<RowRoles>::kOffBRaw + kBStages * kURawBytes + 1024;
+static_assert(kSmemColumn <= 220 * 1024 && kSmemRow <= 220 * 1024, "shared memory budget");
+static_assert(ColRoles::kAStages <= kMaxAStages && RowRoles::kAStages <= kMaxAStages, "stage count");
 
 struct Arena {
     const int32_t* perm;
@@ -208,6 +227,17 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+// Store 16 FP32 columns of this warp's 32 tensor-memory lanes.
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const float (&v)[16]) {
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(taddr),
+        "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])), "r"(__float_as_uint(v[3])),
+        "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])), "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7])),
+        "r"(__float_as_uint(v[8])), "r"(__float_as_uint(v[9])), "r"(__float_as_uint(v[10])), "r"(__float_as_uint(v[11])),
+        "r"(__float_as_uint(v[12])), "r"(__float_as_uint(v[13])), "r"(__float_as_uint(v[14])), "r"(__float_as_uint(v[15]))
+        : "memory");
+}
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
 __device__ __forceinline__ uint32_t prmt(uint32_t a, uint32_t b, uint32_t sel) {
     uint32_t r;
@@ -317,7 +347,7 @@ __device__ __forceinline__ void convert_u(const float* raw, uint8_t* tile, int p
 
 // Shared state of one block.
 struct Shared {
-    uint64_t a_full[kAStages], a_conv[kAStages], a_empty[kAStages];
+    uint64_t a_full[kMaxAStages], a_conv[kMaxAStages], a_empty[kMaxAStages];
     uint64_t b_full[kBStages], b_conv[kBStages], b_empty[kBStages];
     uint64_t acc_full[2], acc_empty[2];
     uint64_t drain;
@@ -331,15 +361,15 @@ struct Shared {
     float fdscale[kPfMaxRhs];  // row kernel: 2^(E_r - 1037) (dense sums, times 2^dense_exp)
 };
 
-__device__ __forceinline__ void init_barriers(Shared& S) {
-    for (int i = 0; i < kAStages; ++i) {
+__device__ __forceinline__ void init_barriers(Shared& S, int astages, int conv_warps) {
+    for (int i = 0; i < astages; ++i) {
         mbar_init(&S.a_full[i], 1);
-        mbar_init(&S.a_conv[i], kConvWarps);
+        mbar_init(&S.a_conv[i], conv_warps);
         mbar_init(&S.a_empty[i], 1);
     }
     for (int i = 0; i < kBStages; ++i) {
         mbar_init(&S.b_full[i], 1);
-        mbar_init(&S.b_conv[i], kConvWarps);
+        mbar_init(&S.b_conv[i], conv_warps);
         mbar_init(&S.b_empty[i], 1);
     }
     for (int i = 0; i < 2; ++i) {
@@ -398,15 +428,19 @@ __global__ void __launch_bounds__(256) pf_xlimbs_kernel(const double* __restrict
 // ------------------------------------------------------------ column kernel
 
 // Persistent: block g runs column items col_sched[g] .. col_sched[g+1].
-__global__ void __launch_bounds__(kThreads, 1) pf_column_kernel(Arena A, Work W, const __grid_constant__ CUtensorMap xmap,
-                                                                int p, int N, int pu, int* status) {
+__global__ void __launch_bounds__(ColRoles::kThreads, 1) pf_column_kernel(Arena A, Work W,
+                                                                          const __grid_constant__ CUtensorMap xmap,
+                                                                          int p, int N, int pu, int* status) {
+    constexpr int kConvWarps = ColRoles::kConvWarps, kEpiWarp0 = ColRoles::kEpiWarp0, kAStages = ColRoles::kAStages;
+    constexpr int kOffAF16 = SmemMap<ColRoles>::kOffAF16, kOffBF16 = SmemMap<ColRoles>::kOffBF16,
+                  kOffARaw = SmemMap<ColRoles>::kOffARaw;
     extern __shared__ uint8_t smem_dyn[];
     uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_dyn) + 1023) & ~uintptr_t(1023));
     __shared__ Shared S;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int it0 = __ldg(A.col_sched + blockIdx.x), it1 = __ldg(A.col_sched + blockIdx.x + 1);
     if (tid == 0) {
-        init_barriers(S);
+        init_barriers(S, kAStages, kConvWarps);
         S.abort_flag = 0;
     }
     if (tid < kPfMaxRhs) {
@@ -590,15 +624,19 @@ __global__ void __launch_bounds__(kThreads, 1) pf_column_kernel(Arena A, Work W,
 
 // ------------------------------------------------------------ row kernel
 
-__global__ void __launch_bounds__(kThreads, 1) pf_row_kernel(Arena A, Work W, const __grid_constant__ CUtensorMap xmap,
-                                                             int p, int N, int pu, int u_beta, int* status) {
+__global__ void __launch_bounds__(RowRoles::kThreads, 1) pf_row_kernel(Arena A, Work W,
+                                                                       const __grid_constant__ CUtensorMap xmap, int p,
+                                                                       int N, int pu, int u_beta, int* status) {
+    constexpr int kConvWarps = RowRoles::kConvWarps, kEpiWarp0 = RowRoles::kEpiWarp0, kAStages = RowRoles::kAStages;
+    constexpr int kOffAF16 = SmemMap<RowRoles>::kOffAF16, kOffBF16 = SmemMap<RowRoles>::kOffBF16,
+                  kOffARaw = SmemMap<RowRoles>::kOffARaw, kOffBRaw = SmemMap<RowRoles>::kOffBRaw;
     extern __shared__ uint8_t smem_dyn[];
     uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_dyn) + 1023) & ~uintptr_t(1023));
     __shared__ Shared S;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int it0 = __ldg(A.row_sched + blockIdx.x), it1 = __ldg(A.row_sched + blockIdx.x + 1);
     if (tid == 0) {
-        init_barriers(S);
+        init_barriers(S, kAStages, kConvWarps);
         S.abort_flag = 0;
     }
     if (tid < kPfMaxRhs) {
@@ -614,7 +652,7 @@ __global__ void __launch_bounds__(kThreads, 1) pf_row_kernel(Arena A, Work W, co
     }
     // B rows 3p .. N-1 of both f16 B stages stay zero (the converters write
     // only rows < 3p; tensor copies of x write zeros there)
-    for (int idx = tid; idx < kBStages * (N - 3 * p) * 8; idx += kThreads) {
+    for (int idx = tid; idx < kBStages * (N - 3 * p) * 8; idx += RowRoles::kThreads) {
         const int s = idx / ((N - 3 * p) * 8), rest = idx % ((N - 3 * p) * 8);
         const int row = 3 * p + rest / 8, c = rest % 8;
         *reinterpret_cast<uint4*>(sm + kOffBF16 + s * kBTileBytes + swz_chunk(row, c)) = make_uint4(0u, 0u, 0u, 0u);
@@ -756,16 +794,25 @@ __global__ void __launch_bounds__(kThreads, 1) pf_row_kernel(Arena A, Work W, co
         }
     } else {
         // ---- epilogue: each segment's sums, scaled (2^-ku for low rank,
-        // 2^(dense_exp + E_r - 1037) for dense), added into FP32 registers;
-        // the item's partial y stored in FP64
+        // 2^(dense_exp + E_r - 1037) for dense), added into FP32 sums kept in
+        // tensor memory (columns 192..255, which no MMA writes: N <= 192 and
+        // the second accumulator starts at 256); the item's partial y stored
+        // in FP64
         const int q = warp & 3, j = 32 * q + lane;
+        const uint32_t yb = tmem + (uint32_t(32 * q) << 16) + 192u;
         unsigned seg = 0;
         bool ok = true;
         for (int it = it0; it < it1 && ok; ++it) {
             const PfRowItem I = A.row_items[it];
-            float y[kPfMaxRhs];
+            {
+                float z[16];
 #pragma unroll
-            for (int r = 0; r < kPfMaxRhs; ++r) y[r] = 0.0f;
+                for (int i = 0; i < 16; ++i) z[i] = 0.0f;
+#pragma unroll
+                for (int g = 0; g < kPfMaxRhs / 16; ++g)
+                    if (16 * g < p) tmem_st16(yb + 16 * g, z);
+                tmem_wait_st();
+            }
             const float dexp = ldexpf(1.0f, max(-126, min(127, I.dense_exp)));
             int c = 0;
             while (c < I.nchunks) {
@@ -778,13 +825,14 @@ __global__ void __launch_bounds__(kThreads, 1) pf_row_kernel(Arena A, Work W, co
                 ++seg;
                 tc_fence_after();
                 const uint32_t base = tmem + (uint32_t(32 * q) << 16) + uint32_t(buf * kAccStride);
-#pragma unroll
+#pragma unroll 1
                 for (int g = 0; g < kPfMaxRhs / 16; ++g) {
                     if (16 * g >= p) break;
-                    float v0[16], v1[16], v2[16];
+                    float v0[16], v1[16], v2[16], y[16];
                     tmem_ld16(base + 48 * g, v0);
                     tmem_ld16(base + 48 * g + 16, v1);
                     tmem_ld16(base + 48 * g + 32, v2);
+                    tmem_ld16(yb + 16 * g, y);
                     tmem_wait_ld();
 #pragma unroll
                     for (int i = 0; i < 16; ++i) {
@@ -794,19 +842,28 @@ __global__ void __launch_bounds__(kThreads, 1) pf_row_kernel(Arena A, Work W, co
                         const float a1 = c1 < 16 ? v0[c1] : (c1 < 32 ? v1[c1 - 16] : v2[c1 - 32]);
                         const float a2 = c2 < 16 ? v0[c2] : (c2 < 32 ? v1[c2 - 16] : v2[c2 - 32]);
                         const float sc = kind == 0 ? S.flscale[r] : S.fdscale[r] * dexp;
-                        y[r] = fmaf((a0 + a1) + a2, sc, y[r]);
+                        y[i] = fmaf((a0 + a1) + a2, sc, y[i]);
                     }
+                    tmem_st16(yb + 16 * g, y);
                 }
+                tmem_wait_st();
                 tc_fence_before();
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&S.acc_empty[buf]);
             }
             if (!ok) break;
-            if (j < I.rows) {
-                double* out = W.part + ((long long)I.part * kPfM + j) * pu;
+            double* out = W.part + ((long long)I.part * kPfM + j) * pu;
+#pragma unroll 1
+            for (int g = 0; g < kPfMaxRhs / 16; ++g) {
+                if (16 * g >= p) break;
+                float y[16];
+                tmem_ld16(yb + 16 * g, y);
+                tmem_wait_ld();
+                if (j < I.rows) {
 #pragma unroll
-                for (int r = 0; r < kPfMaxRhs; ++r)
-                    if (r < p) out[r] = double(y[r]);
+                    for (int i = 0; i < 16; ++i)
+                        if (16 * g + i < p) out[16 * g + i] = double(y[i]);
+                }
             }
         }
     }
@@ -947,9 +1004,9 @@ int pf_pass(const qh_pmatrix* m, const double* x, double* y, int p, long long ld
     pf::pf_xlimbs_kernel<<<(P.n_ent + 255) / 256, 256, 0, s>>>(x, ld, n, p, P.n_ent, P.N, m->A.perm, W.ex, W.xt);
     mark(1);
     if (L.n_col_items > 0)
-        pf::pf_column_kernel<<<L.grid, pf::kThreads, pf::kSmemColumn, s>>>(m->A, W, map, p, P.N, P.pu, status);
+        pf::pf_column_kernel<<<L.grid, pf::ColRoles::kThreads, pf::kSmemColumn, s>>>(m->A, W, map, p, P.N, P.pu, status);
     mark(2);
-    pf::pf_row_kernel<<<L.grid, pf::kThreads, pf::kSmemRow, s>>>(m->A, W, map, p, P.N, P.pu, L.u_beta, status);
+    pf::pf_row_kernel<<<L.grid, pf::RowRoles::kThreads, pf::kSmemRow, s>>>(m->A, W, map, p, P.N, P.pu, L.u_beta, status);
     mark(3);
     const long long total = (long long)n * p;
     pf::pf_combine_kernel<<<unsigned((total + 255) / 256), 256, 0, s>>>(m->A.perm, m->tile_part0, W.part, y, ld, n,
