@@ -354,7 +354,7 @@ def run_reference_arm(args):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": model / (base["value"] * 1e9) * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": DATA_NOTE,
-        "config": _config(args.workload, wl, build_s),
+        "config": _config(args.workload, wl), "construction_s": round(build_s, 1),
         "cpu_baseline": base,
         "e2e": {"value": base["value"], "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -384,14 +384,13 @@ METRIC = "H-matvec GB/s (% HBM peak)"
 DATA_NOTE = "synthetic (seeded points; matrix constructed on the host)"
 
 
-def _config(name, wl, build_s):
+def _config(name, wl):
     """The workload description, identical in both arms."""
     return {"workload": f"{name}: {wl['desc']}", "n": wl["n"], "rhs": wl["rhs"],
             "tolerance": wl["tol"], "tolerance_requested": wl["tol_requested"],
             "tolerance_note": ("requested tolerance infeasible in the reference; tightest feasible of "
                                "the ladder 1e-8/3e-8/1e-7/3e-7/1e-6") if wl["tol"] != wl["tol_requested"] else "",
-            "l2": "representation larger than L2 (129 MB; 1.3 GB for the precision workload); no flush between steps",
-            "construction_s": round(build_s, 1)}
+            "l2": "representation larger than L2 (129 MB; 1.3 GB for the precision workload); no flush between steps"}
 
 
 def dense_oracle_error(pts, kernel: str, x, y, device) -> dict:
@@ -561,7 +560,7 @@ def run_precision(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f16 digit planes x f16 hi/mid/lo limbs of x and u, f32 accumulate (tcgen05, TMEM); "
                  "f64 scales, dense-limb sums and y",
-        "data": DATA_NOTE, "config": _config(args.workload, wl, build_s),
+        "data": DATA_NOTE, "config": _config(args.workload, wl), "construction_s": round(build_s, 1),
         "roofline": {"bound": bound, "kernel": dom, "achieved": round(achieved, 1),
                      "peak": tc_peak if bound == "tensor" else hbm_peak,
                      "unit": "TFLOP/s" if bound == "tensor" else "GB/s",
@@ -1090,7 +1089,7 @@ def main():
         "dtype": "f64 (int2..int32 codes x 62-bit fixed-point x/u, exact f16 tensor-core digit x limb products; "
                  "FP64 scales, diagonal)",
         "data": DATA_NOTE,
-        "config": _config(args.workload, wl, build_s),
+        "config": _config(args.workload, wl), "construction_s": round(build_s, 1),
         "workload_stats": {"parallelism": f"replicas x{world}", "model_bytes": model, "components": comps,
                            "blocks": st["block_count"]},
         "pct_hbm_peak": round(100 * value / world / peak, 1),

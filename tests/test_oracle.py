@@ -185,5 +185,7 @@ def test_reference_arm_never_loads_the_cuda_library():
     assert lines[-1] == "MAPS 0"
     out = json.loads(lines[-2])
     assert out["impl"] == "reference" and out["e2e"]["h2d_bytes_per_step"] == 0
+    # the config is the workload alone (equal in both arms); timings sit outside it
     assert set(out["config"]) == {"workload", "n", "rhs", "tolerance", "tolerance_requested",
-                                  "tolerance_note", "l2", "construction_s"}
+                                  "tolerance_note", "l2"}
+    assert "construction_s" in out
