@@ -601,7 +601,9 @@ def run_precision(args):
         e2e = (time.perf_counter() - t0) / ne
         out["e2e"] = {"value": round(rhs / e2e, 1), "unit": "RHS/s", "h2d_bytes_per_step": int(xh.nbytes),
                       "d2h_bytes_per_step": int(yh.nbytes), "ms_per_step": round(1e3 * e2e, 4),
-                      "transfer": "pageable NumPy X copied to the device, Y copied back, per call"}
+                      "transfer": ("qh_pmatmul_host: X read and Y written by the kernels in the caller's NumPy "
+                                   "buffers over the coherent host link" if pf.host_direct else
+                                   "qh_pmatmul_host: pinned staging, one H2D copy of X and one D2H copy of Y")}
         if not args.no_cpu_baseline:
             from oracle import oracle
 

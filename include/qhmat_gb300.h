@@ -259,6 +259,19 @@ QH_API int qh_pmatmul_device_profiled(const qh_pmatrix* m, const double* x, doub
                                       void* workspace, size_t workspace_bytes, void* stream, int* status,
                                       void* const* events5);
 
+/* y = A x in the precision form with x and y in host memory (row-major
+ * order x rhs, source order), as qh_matmul_host is for the plain form: on a
+ * device that reaches pageable host memory through the host's page tables
+ * (GB300 on its Grace host) the kernels read x and write y in the caller's
+ * buffers directly, elsewhere they are staged through pinned memory with one
+ * copy each way.  Synchronous; the checks and messages of qh_matmul_host.
+ * The precision-form counterpart of the reference's matmul_cuda
+ * (src/qhmat/cuda.cu:106-164) for many right-hand sides. */
+QH_API int qh_pmatmul_host(const qh_pmatrix* m, const double* x, double* y, size_t rhs);
+/* 1 when qh_pmatmul_host reads and writes host buffers in place on this
+ * handle's device, 0 when it stages them. */
+QH_API int qh_pmatrix_host_direct(const qh_pmatrix* m);
+
 /* ---- Batched applies (serving): column gather / scatter ----
  *
  * The reference applies one request at a time and copies every operand per

@@ -94,6 +94,10 @@ def load_library() -> C.CDLL:
     lib.qh_pworkspace_bytes.argtypes = [vp, sz]
     lib.qh_pmatmul_device.restype = i32
     lib.qh_pmatmul_device.argtypes = [vp, vp, vp, sz, vp, sz, vp, vp]
+    lib.qh_pmatmul_host.restype = i32
+    lib.qh_pmatmul_host.argtypes = [vp, vp, vp, sz]
+    lib.qh_pmatrix_host_direct.restype = i32
+    lib.qh_pmatrix_host_direct.argtypes = [vp]
     lib.qh_pmatmul_device_profiled.restype = i32
     lib.qh_pmatmul_device_profiled.argtypes = [vp, vp, vp, sz, vp, sz, vp, vp, vp]
     ll = C.c_longlong

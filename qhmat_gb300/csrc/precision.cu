@@ -47,6 +47,8 @@
 #include <string>
 #include <vector>
 
+#include <unistd.h>
+
 #include "../../include/qhmat_gb300.h"
 #include "errors.hpp"
 #include "layout.hpp"
@@ -904,6 +906,15 @@ struct qh_pmatrix {
     std::mutex mu;
     void* own_ws = nullptr;
     size_t own_ws_bytes = 0;
+    // qh_pmatmul_host: its stream, status word, pinned staging (devices
+    // that cannot reach pageable host memory) and whether the kernels may
+    // read x and write y in the caller's memory directly
+    cudaStream_t stream = nullptr;
+    int* d_status = nullptr;
+    int* h_status = nullptr;
+    void* pinned = nullptr;
+    size_t pinned_bytes = 0;
+    int host_direct = -1;  // -1: not probed yet
     ~qh_pmatrix() {
         int prev = 0;
         cudaGetDevice(&prev);
@@ -911,6 +922,10 @@ struct qh_pmatrix {
         if (arena) cudaFree(arena);
         if (tile_part0) cudaFree(tile_part0);
         if (own_ws) cudaFree(own_ws);
+        if (d_status) cudaFree(d_status);
+        if (h_status) cudaFreeHost(h_status);
+        if (pinned) cudaFreeHost(pinned);
+        if (stream) cudaStreamDestroy(stream);
         cudaSetDevice(prev);
     }
 };
@@ -1178,6 +1193,94 @@ int qh_pmatmul_device_profiled(const qh_pmatrix* m, const double* x, double* y, 
         if (rc) return rc;
     }
     return QH_OK;
+}
+
+
+int qh_pmatmul_host(const qh_pmatrix* m, const double* x, double* y, size_t rhs) {
+    if (!m) return set_error(QH_EINVAL, "null matrix handle");
+    if (rhs == 0 || rhs > SIZE_MAX / m->L.order / sizeof(double))
+        return set_error(QH_EINVAL, "right-hand-side shape mismatch");
+    if (m->L.order * rhs > size_t(INT32_MAX) * 256) return set_error(QH_EOVERFLOW, "CUDA launch grid too large");
+    if (!x || !y) return set_error(QH_EINVAL, "null right-hand side or result pointer");
+    Guard g(m->device);
+    auto* mm = const_cast<qh_pmatrix*>(m);
+    std::lock_guard<std::mutex> lock(mm->mu);
+    cudaError_t e;
+    if (mm->host_direct < 0) {
+        int pageable = 0, host_tables = 0;
+        cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, m->device);
+        cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, m->device);
+        mm->host_direct = pageable == 1 && host_tables == 1 ? 1 : 0;
+    }
+    if (!mm->stream && (e = cudaStreamCreateWithFlags(&mm->stream, cudaStreamNonBlocking)) != cudaSuccess)
+        return cuda_err(e, "cudaStreamCreate");
+    if (!mm->d_status) {
+        if ((e = cudaMalloc(&mm->d_status, sizeof(int))) != cudaSuccess) return cuda_err(e, "cudaMalloc");
+        if ((e = cudaMallocHost(&mm->h_status, sizeof(int))) != cudaSuccess) return cuda_err(e, "cudaMallocHost");
+    }
+    const size_t vec = m->L.order * rhs * sizeof(double);
+    const size_t need_ws = pf_plan(m->L, rhs).total;
+    const auto* xb = reinterpret_cast<const uint8_t*>(x);
+    const auto* yb = reinterpret_cast<const uint8_t*>(y);
+    const bool direct = mm->host_direct == 1 && (xb + vec <= yb || yb + vec <= xb);
+    // device buffer: workspace [| x | y when staged]
+    const size_t need = direct ? need_ws : a256(need_ws) + 2 * a256(vec);
+    if (mm->own_ws_bytes < need) {
+        if (mm->own_ws) cudaFree(mm->own_ws);
+        mm->own_ws = nullptr;
+        mm->own_ws_bytes = 0;
+        if ((e = cudaMalloc(&mm->own_ws, need)) != cudaSuccess) return cuda_err(e, "cudaMalloc");
+        mm->own_ws_bytes = need;
+    }
+    auto* base = static_cast<uint8_t*>(mm->own_ws);
+    const double* dx = x;
+    double* dy = y;
+    if (direct) {
+        // one write per page of y makes every page present and writable before
+        // the device writes it
+        static const uintptr_t page = uintptr_t(sysconf(_SC_PAGESIZE) > 0 ? sysconf(_SC_PAGESIZE) : 4096);
+        const uintptr_t y0 = reinterpret_cast<uintptr_t>(y), y1 = y0 + vec;
+        for (uintptr_t a = y0; a < y1; a = (a & ~(page - 1)) + page) *reinterpret_cast<volatile uint8_t*>(a) = 0;
+    } else {
+        if (mm->pinned_bytes < vec) {
+            if (mm->pinned) cudaFreeHost(mm->pinned);
+            mm->pinned = nullptr;
+            mm->pinned_bytes = 0;
+            if ((e = cudaMallocHost(&mm->pinned, vec)) != cudaSuccess) return cuda_err(e, "cudaMallocHost");
+            mm->pinned_bytes = vec;
+        }
+        double* sx = reinterpret_cast<double*>(base + a256(need_ws));
+        dy = reinterpret_cast<double*>(base + a256(need_ws) + a256(vec));
+        dx = sx;
+        std::memcpy(mm->pinned, x, vec);
+        if ((e = cudaMemcpyAsync(sx, mm->pinned, vec, cudaMemcpyHostToDevice, mm->stream)) != cudaSuccess)
+            return cuda_err(e, "cudaMemcpy host-to-device");
+    }
+    if ((e = cudaMemsetAsync(mm->d_status, 0, sizeof(int), mm->stream)) != cudaSuccess)
+        return cuda_err(e, "cudaMemsetAsync");
+    for (size_t c0 = 0; c0 < rhs; c0 += kPfMaxRhs) {
+        const int p = int(std::min<size_t>(kPfMaxRhs, rhs - c0));
+        const int rc = pf_pass(m, dx + c0, dy + c0, p, (long long)rhs, base, mm->stream, mm->d_status, nullptr);
+        if (rc) return rc;
+    }
+    if (!direct && (e = cudaMemcpyAsync(mm->pinned, dy, vec, cudaMemcpyDeviceToHost, mm->stream)) != cudaSuccess)
+        return cuda_err(e, "cudaMemcpy device-to-host");
+    if ((e = cudaMemcpyAsync(mm->h_status, mm->d_status, sizeof(int), cudaMemcpyDeviceToHost, mm->stream)) !=
+        cudaSuccess)
+        return cuda_err(e, "cudaMemcpy device-to-host");
+    if ((e = cudaStreamSynchronize(mm->stream)) != cudaSuccess) return cuda_err(e, "CUDA kernel execution");
+    if (*mm->h_status & QH_STATUS_NONFINITE) return set_error(QH_EINVAL, "nonfinite right-hand side");
+    if (*mm->h_status & QH_STATUS_TIMEOUT) return set_error(QH_ERUNTIME, "device copy wait timed out");
+    if (!direct) std::memcpy(y, mm->pinned, vec);
+    return QH_OK;
+}
+
+int qh_pmatrix_host_direct(const qh_pmatrix* m) {
+    if (!m) return set_error(QH_EINVAL, "null matrix handle");
+    int pageable = 0, host_tables = 0;
+    cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, m->device);
+    cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, m->device);
+    return pageable == 1 && host_tables == 1 ? 1 : 0;
 }
 
 }  // extern "C"

@@ -299,20 +299,33 @@ class PrecisionHMatrix:
     def workspace_bytes(self, rhs: int) -> int:
         return int(self._lib.qh_pworkspace_bytes(self._h, rhs))
 
+    @property
+    def host_direct(self) -> bool:
+        """True when NumPy applies read x and write y in host memory in place
+        (the device walks the host's page tables), False when staged."""
+        return bool(self._lib.qh_pmatrix_host_direct(self._h))
+
     def matmul(self, x, *, stream=None, workspace=None, check: bool = True):
-        """Apply to ``(n,)`` or ``(n, p)`` FP64 input (NumPy: copied to the
-        device and back; CUDA torch tensor: on ``stream``, result a tensor)."""
-        torch = _torch()
-        numpy_in = not _is_torch_tensor(x)
-        if numpy_in:
+        """Apply to ``(n,)`` or ``(n, p)`` FP64 input (NumPy: through
+        ``qh_pmatmul_host``, a new NumPy result; CUDA torch tensor: on
+        ``stream``, result a tensor)."""
+        if not _is_torch_tensor(x):
             a = np.ascontiguousarray(np.asarray(x, dtype=np.float64))
-            xt = torch.from_numpy(a).to(torch.device("cuda", self._device))
-        else:
-            xt = x
-            if not xt.is_cuda or xt.device.index != self._device:
-                raise ValueError(f"tensor right-hand side must live on cuda:{self._device}")
-            if xt.dtype != torch.float64:
-                raise ValueError("tensor right-hand side must be torch.float64")
+            if a.ndim not in (1, 2):
+                raise ValueError("right-hand side must be one- or two-dimensional")
+            if a.shape[0] != self.order:
+                raise ValueError("right-hand side has the wrong row count")
+            rhs = 1 if a.ndim == 1 else int(a.shape[1])
+            y = np.empty_like(a)
+            if a.size:
+                raise_for(self._lib.qh_pmatmul_host(self._h, a.ctypes.data, y.ctypes.data, rhs))
+            return y
+        torch = _torch()
+        xt = x
+        if not xt.is_cuda or xt.device.index != self._device:
+            raise ValueError(f"tensor right-hand side must live on cuda:{self._device}")
+        if xt.dtype != torch.float64:
+            raise ValueError("tensor right-hand side must be torch.float64")
         shape = tuple(xt.shape)
         if len(shape) not in (1, 2):
             raise ValueError("right-hand side must be one- or two-dimensional")
@@ -330,13 +343,13 @@ class PrecisionHMatrix:
         s = stream if stream is not None else torch.cuda.current_stream(xt.device)
         raise_for(self._lib.qh_pmatmul_device(self._h, xt.data_ptr(), y.data_ptr(), rhs, workspace.data_ptr(),
                                               need, s.cuda_stream, status.data_ptr()))
-        if check or numpy_in:
+        if check:
             st = int(status.item())
             if st & QH_STATUS_NONFINITE:
                 raise ValueError("nonfinite right-hand side")
             if st & QH_STATUS_TIMEOUT:
                 raise RuntimeError("device copy wait timed out")
-        return y.cpu().numpy() if numpy_in else y
+        return y
 
 
 def precision_gate(y_form, y_plain, x, bound: float) -> dict:

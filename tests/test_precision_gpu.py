@@ -74,6 +74,30 @@ def test_precision_form_is_deterministic_and_column_independent(cuda_device):
     assert rel_err(y5.cpu().numpy(), y1[:, 5].cpu().numpy()) <= 1e-12
 
 
+def test_host_buffers_match_device_buffers(cuda_device):
+    """qh_pmatmul_host (NumPy buffers: read and written in place by the
+    kernels on a device that walks the host page tables, else staged through
+    pinned memory) gives the tensor path's y bit for bit; an in-place call
+    (x and y the same buffer) takes the staged path and agrees as well."""
+    import ctypes as C
+
+    import torch
+
+    from qhmat_gb300 import _lib
+
+    data, _ = golden("ragged300")
+    pm = PrecisionHMatrix.from_bytes(data)
+    x = np.random.default_rng(8).standard_normal((300, 70))
+    y_dev = pm.matmul(torch.from_numpy(x).cuda()).cpu().numpy()
+    y_host = pm.matmul(x)
+    assert np.array_equal(y_host, y_dev)
+    buf = x.copy()
+    lib = _lib.load_library()
+    _lib.raise_for(lib.qh_pmatmul_host(pm._h, buf.ctypes.data, buf.ctypes.data, C.c_size_t(70)))
+    assert np.array_equal(buf, y_dev)
+    assert pm.host_direct in (True, False)
+
+
 def test_precision_form_large_blocks_p64(cuda_device):
     """1-D n = 4096, -log(r + 1e-3), tolerance 1e-6: blocks up to 1024 columns,
     64 right-hand sides in one pass."""
