@@ -874,6 +874,23 @@ __global__ void __launch_bounds__(RowRoles::kThreads, 1) pf_row_kernel(Arena A, 
     if (warp == 1) tmem_free(tmem, 512);
 }
 
+// dst[i] = src[i], i < n: one pass of wide, independent loads, so that x in
+// the caller's host memory crosses the host link once at full width (the
+// exponent and limb kernels then read the device copy).
+__global__ void __launch_bounds__(256) pf_copy_kernel(const double* __restrict__ src, double* __restrict__ dst,
+                                                      size_t n) {
+    const size_t stride = size_t(gridDim.x) * blockDim.x;
+    size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    for (; i + 3 * stride < n; i += 4 * stride) {
+        const double a = src[i], b = src[i + stride], c = src[i + 2 * stride], d = src[i + 3 * stride];
+        dst[i] = a;
+        dst[i + stride] = b;
+        dst[i + 2 * stride] = c;
+        dst[i + 3 * stride] = d;
+    }
+    for (; i < n; i += stride) dst[i] = src[i];
+}
+
 // y[perm[row] * ld + r] = the tile's partials, summed in K-split order.
 __global__ void __launch_bounds__(256) pf_combine_kernel(const int32_t* __restrict__ perm,
                                                          const int32_t* __restrict__ tile_part0,
@@ -1223,8 +1240,8 @@ int qh_pmatmul_host(const qh_pmatrix* m, const double* x, double* y, size_t rhs)
     const auto* xb = reinterpret_cast<const uint8_t*>(x);
     const auto* yb = reinterpret_cast<const uint8_t*>(y);
     const bool direct = mm->host_direct == 1 && (xb + vec <= yb || yb + vec <= xb);
-    // device buffer: workspace [| x | y when staged]
-    const size_t need = direct ? need_ws : a256(need_ws) + 2 * a256(vec);
+    // device buffer: workspace | x [| y when staged]
+    const size_t need = a256(need_ws) + (direct ? a256(vec) : 2 * a256(vec));
     if (mm->own_ws_bytes < need) {
         if (mm->own_ws) cudaFree(mm->own_ws);
         mm->own_ws = nullptr;
@@ -1241,6 +1258,13 @@ int qh_pmatmul_host(const qh_pmatrix* m, const double* x, double* y, size_t rhs)
         static const uintptr_t page = uintptr_t(sysconf(_SC_PAGESIZE) > 0 ? sysconf(_SC_PAGESIZE) : 4096);
         const uintptr_t y0 = reinterpret_cast<uintptr_t>(y), y1 = y0 + vec;
         for (uintptr_t a = y0; a < y1; a = (a & ~(page - 1)) + page) *reinterpret_cast<volatile uint8_t*>(a) = 0;
+        // x: one device copy, read across the host link once
+        double* sx = reinterpret_cast<double*>(base + a256(need_ws));
+        const size_t nx = m->L.order * rhs;
+        const unsigned blocks = unsigned(std::min<size_t>((nx + 255) / 256, size_t(m->sms) * 8));
+        pf::pf_copy_kernel<<<std::max(1u, blocks), 256, 0, mm->stream>>>(x, sx, nx);
+        if ((e = cudaGetLastError()) != cudaSuccess) return cuda_err(e, "CUDA kernel launch");
+        dx = sx;
     } else {
         if (mm->pinned_bytes < vec) {
             if (mm->pinned) cudaFreeHost(mm->pinned);
