@@ -620,8 +620,25 @@ __device__ __forceinline__ void dense_unit(const Arena& A, const Work& W, const 
     const double* col = A.dense + D.off + (long long)u.chunk0 * D.ld + lane;
     const double* xv = W.xc + (long long)p * n + D.xcol + u.chunk0;
     double s0 = 0.0, s1 = 0.0;
-#pragma unroll 4
-    for (int k = 0; k < u.n; ++k) {
+    // batches of eight columns: every load of a batch is issued before its
+    // FMAs (the dense data comes from HBM); rows past the tile read 0 and add
+    // nothing (fma(0, x, s) = s for finite x)
+    int k = 0;
+    for (; k + 8 <= u.n; k += 8) {
+        double c0[8], c1[8], xk[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            xk[i] = __ldcg(xv + k + i);
+            c0[i] = r0 ? __ldg(col + (long long)(k + i) * D.ld) : 0.0;
+            c1[i] = r1 ? __ldg(col + (long long)(k + i) * D.ld + 32) : 0.0;
+        }
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            s0 = fma(c0[i], xk[i], s0);
+            s1 = fma(c1[i], xk[i], s1);
+        }
+    }
+    for (; k < u.n; ++k) {
         const double xk = __ldcg(xv + k);
         if (r0) s0 = fma(__ldg(col + (long long)k * D.ld), xk, s0);
         if (r1) s1 = fma(__ldg(col + (long long)k * D.ld + 32), xk, s1);

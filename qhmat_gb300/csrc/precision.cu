@@ -158,6 +158,11 @@ __device__ __forceinline__ bool wait_bar(uint64_t* bar, unsigned parity, volatil
     if (status) atomicOr(status, kStatusTimeout);
     return false;
 }
+// Pull a descriptor two items (chunks) ahead into L1, so that the roles that
+// read it find it there instead of waiting for L2 at every item.
+__device__ __forceinline__ void prefetch_l1(const void* ptr) {
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(ptr));
+}
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
 __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
@@ -464,6 +469,7 @@ __global__ void __launch_bounds__(ColRoles::kThreads, 1) pf_column_kernel(Arena 
             bool ok = true;
             for (int it = it0; it < it1 && ok; ++it) {
                 const PfColItem I = A.col_items[it];
+                if (it + 2 < it1) prefetch_l1(A.col_items + it + 2);
                 for (int kc = 0; kc < I.nkc && ok; ++kc) {
                     const int sb = bi % kBStages;
                     if (bi >= kBStages) ok = wait_bar(&S.b_empty[sb], ((bi / kBStages) - 1) & 1, abort_flag, status);
@@ -500,6 +506,7 @@ __global__ void __launch_bounds__(ColRoles::kThreads, 1) pf_column_kernel(Arena 
             bool ok = true;
             for (int it = it0; it < it1 && ok; ++it) {
                 const PfColItem I = A.col_items[it];
+                if (it + 2 < it1) prefetch_l1(A.col_items + it + 2);
                 for (int kc0 = 0; kc0 < I.nkc && ok; kc0 += kSegChunks, ++seg) {
                     const int buf = seg & 1;
                     if (seg >= 2) ok = wait_bar(&S.acc_empty[buf], ((seg >> 1) - 1) & 1, abort_flag, status);
@@ -543,6 +550,7 @@ __global__ void __launch_bounds__(ColRoles::kThreads, 1) pf_column_kernel(Arena 
         bool ok = true;
         for (int it = it0; it < it1 && ok; ++it) {
             const PfColItem I = A.col_items[it];
+            if (it + 2 < it1) prefetch_l1(A.col_items + it + 2);
             for (int kc = 0; kc < I.nkc && ok; ++kc)
                 for (int m = 0; m < I.planes; ++m) {
                     const int sa = ai % kAStages;
@@ -566,6 +574,7 @@ __global__ void __launch_bounds__(ColRoles::kThreads, 1) pf_column_kernel(Arena 
         bool ok = true;
         for (int it = it0; it < it1 && ok; ++it) {
             const PfColItem I = A.col_items[it];
+            if (it + 2 < it1) prefetch_l1(A.col_items + it + 2);
             PfComp C{};
             if (j < I.count) C = A.comps[I.comp0 + j];
             const float sf = float(C.scale);
@@ -675,6 +684,7 @@ __global__ void __launch_bounds__(RowRoles::kThreads, 1) pf_row_kernel(Arena A, 
                 const PfRowItem I = A.row_items[it];
                 for (int c = 0; c < I.nchunks && ok; ++c) {
                     const PfRowChunk C = A.chunks[I.chunk0 + c];
+                    if (c + 2 < I.nchunks) prefetch_l1(A.chunks + I.chunk0 + c + 2);
                     const int sb = bi % kBStages;
                     if (bi >= kBStages) ok = wait_bar(&S.b_empty[sb], ((bi / kBStages) - 1) & 1, abort_flag, status);
                     if (!ok) break;
@@ -730,6 +740,7 @@ __global__ void __launch_bounds__(RowRoles::kThreads, 1) pf_row_kernel(Arena A, 
                     int acc = 0;
                     for (; c < c_end && ok; ++c) {
                         const PfRowChunk C = A.chunks[I.chunk0 + c];
+                        if (c + 2 < I.nchunks) prefetch_l1(A.chunks + I.chunk0 + c + 2);
                         const int sb = bi % kBStages;
                         ok = wait_bar(&S.b_conv[sb], (bi / kBStages) & 1, abort_flag, status);
                         if (!ok) break;
@@ -767,6 +778,7 @@ __global__ void __launch_bounds__(RowRoles::kThreads, 1) pf_row_kernel(Arena A, 
             const PfRowItem I = A.row_items[it];
             for (int c = 0; c < I.nchunks && ok; ++c) {
                 const PfRowChunk C = A.chunks[I.chunk0 + c];
+                if (c + 2 < I.nchunks) prefetch_l1(A.chunks + I.chunk0 + c + 2);
                 const int sb = bi % kBStages;
                 ok = wait_bar(&S.b_full[sb], (bi / kBStages) & 1, abort_flag, status);
                 if (!ok) break;
