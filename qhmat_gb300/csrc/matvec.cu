@@ -1963,16 +1963,17 @@ int qh_matmul_host(const qh_matrix* m, const double* x, double* y, size_t rhs) {
             const uintptr_t y0 = reinterpret_cast<uintptr_t>(y), y1 = y0 + vec;
             for (uintptr_t a = y0; a < y1; a = (a & ~(page - 1)) + page) *reinterpret_cast<volatile uint8_t*>(a) = 0;
         }
-        if ((e = cudaMemsetAsync(mm->d_status, 0, sizeof(int), mm->stream)) != cudaSuccess)
-            return cuda_fail(e, "cudaMemsetAsync");
-        rc = launch(m, x, y, rhs, mm->own_ws, mm->stream, mm->d_status);
+        // the status word is the pinned host int itself (device-accessible at
+        // the same address under unified addressing): no memset and no copy
+        // back on the stream
+        volatile int* hs = mm->h_status;
+        *hs = 0;
+        rc = launch(m, x, y, rhs, mm->own_ws, mm->stream, mm->h_status);
         if (rc) return rc;
-        if ((e = cudaMemcpyAsync(mm->h_status, mm->d_status, sizeof(int), cudaMemcpyDeviceToHost, mm->stream)) !=
-            cudaSuccess)
-            return cuda_fail(e, "cudaMemcpy device-to-host");
         if ((e = cudaStreamSynchronize(mm->stream)) != cudaSuccess) return cuda_fail(e, "CUDA kernel execution");
-        if (*mm->h_status & kStatusNonfinite) return fail(QH_EINVAL, "nonfinite right-hand side");
-        if (*mm->h_status & kStatusTimeout) return fail(QH_ERUNTIME, "device copy wait timed out");
+        const int st = *hs;
+        if (st & kStatusNonfinite) return fail(QH_EINVAL, "nonfinite right-hand side");
+        if (st & kStatusTimeout) return fail(QH_ERUNTIME, "device copy wait timed out");
         return QH_OK;
     }
     // one device buffer: workspace | x | y
