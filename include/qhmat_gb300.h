@@ -236,6 +236,7 @@ typedef struct {
     uint64_t mma_elements;      /* M x K elements through the MMAs per pass (x N = 3p limbs) */
     uint64_t launches_per_pass; /* kernels per pass of <= 64 right-hand sides */
     uint64_t mma_col_elements, mma_row_elements; /* the column and row kernels' shares */
+    uint64_t segment_chunks;    /* K chunks per FP32 accumulation segment (1 or 2) */
 } qh_pstats;
 
 /* Parse a QHMAT001 image (the checks and messages of qh_matrix_from_qhmat)
@@ -243,6 +244,12 @@ typedef struct {
 QH_API int qh_pmatrix_from_qhmat(const void* bytes, size_t len, int device, qh_pmatrix** out);
 QH_API void qh_pmatrix_destroy(qh_pmatrix* m);
 QH_API int qh_pmatrix_stats(const qh_pmatrix* m, qh_pstats* out);
+/* K chunks (of 64 entries) that one FP32 accumulation segment spans: 2 (the
+ * default) or 1.  The tensor cores truncate as they accumulate, so shorter
+ * segments halve this form's error (2.4e-7 vs 4.8e-7 relative to the plain
+ * form on an n=32768 x 64 apply) for ~4% more time per pass.  Set it before
+ * applies, not during them.  No reference counterpart. */
+QH_API int qh_pmatrix_set_segment_chunks(qh_pmatrix* m, int chunks);
 /* Device scratch of one qh_pmatmul_device call with `rhs` columns (passes of
  * 64 columns share it). */
 QH_API size_t qh_pworkspace_bytes(const qh_pmatrix* m, size_t rhs);

@@ -29,7 +29,7 @@ class QhPStats(C.Structure):
     _fields_ = [(name, C.c_uint64) for name in (
         "order", "components", "code_bytes", "scale_bytes", "dense_bytes", "stored_q_bytes",
         "stored_p_bytes", "stored_dense_bytes", "device_bytes", "col_items", "row_items", "row_slots",
-        "mma_elements", "launches_per_pass", "mma_col_elements", "mma_row_elements")]
+        "mma_elements", "launches_per_pass", "mma_col_elements", "mma_row_elements", "segment_chunks")]
 
 
 class QhBlockDesc(C.Structure):
@@ -94,6 +94,8 @@ def load_library() -> C.CDLL:
     lib.qh_pworkspace_bytes.argtypes = [vp, sz]
     lib.qh_pmatmul_device.restype = i32
     lib.qh_pmatmul_device.argtypes = [vp, vp, vp, sz, vp, sz, vp, vp]
+    lib.qh_pmatrix_set_segment_chunks.restype = i32
+    lib.qh_pmatrix_set_segment_chunks.argtypes = [vp, C.c_int]
     lib.qh_pmatmul_host.restype = i32
     lib.qh_pmatmul_host.argtypes = [vp, vp, vp, sz]
     lib.qh_pmatrix_host_direct.restype = i32

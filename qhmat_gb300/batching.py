@@ -53,7 +53,7 @@ class _Batch:
     """One block-diagonal handle (plain or precision) over a subset of the
     matrices, with its device table, operand buffers and workspace."""
 
-    def __init__(self, images, orders, rhs, x_offs, device, precision, grid=0, row_items=0.0):
+    def __init__(self, images, orders, rhs, x_offs, device, precision, grid=0, row_items=0.0, seg=2):
         import torch
 
         self.lib = load_library()
@@ -68,6 +68,7 @@ class _Batch:
         if precision:
             raise_for(self.lib.qh_pmatrix_from_batch(ptrs, lens, self.count, device, int(grid), float(row_items),
                                                      C.byref(h), offs))
+            raise_for(self.lib.qh_pmatrix_set_segment_chunks(h, int(seg)))
         else:
             raise_for(self.lib.qh_matrix_from_batch(ptrs, lens, self.count, device, C.byref(h), offs))
         self.h = h
@@ -151,6 +152,7 @@ class BatchedHMatrices:
         self.streams = (torch.cuda.Stream(device=dev), torch.cuda.Stream(device=dev))
         self.form = ["plain"] * len(images)
         self.calibration = []
+        self.pf_seg = 2  # accumulation segment of the precision batch (1 where a matrix needs it)
         # per-matrix reconstruction bounds (for the gate) from the plain handles' metadata
         self.stats = []
         for img in images:
@@ -170,7 +172,7 @@ class BatchedHMatrices:
             params = {"grid": 0, "row_items": 0.0}
             if autotune:
                 params = self._autotune(pf_idx, images, cache)
-            self.batches.append(self._make(images, pf_idx, True, **params))
+            self.batches.append(self._make(images, pf_idx, True, seg=self.pf_seg, **params))
         # plain matrices in sub-batches by right-hand-side count: the plain
         # form's work grows with the columns it is given (every matrix of a
         # sub-batch is applied to its widest column count), so a 3-column
@@ -186,9 +188,9 @@ class BatchedHMatrices:
         self.graph = None
 
     # ------------------------------------------------------------ building
-    def _make(self, images, idx, precision, grid=0, row_items=0.0):
+    def _make(self, images, idx, precision, grid=0, row_items=0.0, seg=2):
         return _Batch([images[k] for k in idx], [self.orders[k] for k in idx], [self.rhs[k] for k in idx],
-                      [int(self.x_offsets[k]) for k in idx], self.device, precision, grid, row_items)
+                      [int(self.x_offsets[k]) for k in idx], self.device, precision, grid, row_items, seg)
 
     def _probe(self, probes):
         import torch
@@ -199,31 +201,38 @@ class BatchedHMatrices:
         return x
 
     def _calibrate(self, images, probes):
-        """Both forms over the whole batch on seeded N(0,1) right-hand sides;
-        a matrix takes the precision form when its worst column's gate ratio
-        is at most 0.5."""
+        """Both forms over the whole batch on seeded N(0,1) right-hand sides
+        (the precision form with two-chunk and with one-chunk accumulation
+        segments); a matrix takes the precision form when its worst column's
+        gate ratio is at most 0.5.  The precision batch uses one-chunk
+        segments when a matrix passes only with them (half the error, ~4%
+        more time), and every matrix is then judged at that setting."""
         import torch
 
         idx = list(range(len(images)))
         x = self._probe(probes)
         outs = []
-        for precision in (False, True):
-            b = self._make(images, idx, precision)
+        for precision, seg in ((False, 2), (True, 2), (True, 1)):
+            b = self._make(images, idx, precision, seg=seg)
             y = torch.zeros_like(x)
             b.apply(x, y, torch.cuda.current_stream(self.dev))
             torch.cuda.synchronize(self.dev)
             outs.append(y.cpu().numpy())
             b.close()
         xh = x.cpu().numpy()
-        forms = []
+        ratios = {2: [], 1: []}
         for k in idx:
             a, b_ = int(self.x_offsets[k]), int(self.x_offsets[k + 1])
             shape = (self.orders[k], self.rhs[k])
-            g = precision_gate(outs[1][a:b_].reshape(shape), outs[0][a:b_].reshape(shape), xh[a:b_].reshape(shape),
-                               self.bounds[k])
-            self.calibration.append(g["worst_ratio"])
-            forms.append("precision" if g["worst_ratio"] <= 0.5 and self.rhs[k] >= 2 else "plain")
-        return forms
+            for seg, y in ((2, outs[1]), (1, outs[2])):
+                g = precision_gate(y[a:b_].reshape(shape), outs[0][a:b_].reshape(shape), xh[a:b_].reshape(shape),
+                                   self.bounds[k])
+                ratios[seg].append(g["worst_ratio"])
+        need_fine = any(r2 > 0.5 and r1 <= 0.5 and self.rhs[k] >= 2
+                        for k, (r2, r1) in enumerate(zip(ratios[2], ratios[1])))
+        self.pf_seg = 1 if need_fine else 2
+        self.calibration = ratios[self.pf_seg]
+        return ["precision" if r <= 0.5 and self.rhs[k] >= 2 else "plain" for k, r in enumerate(self.calibration)]
 
     def _autotune(self, idx, all_images, cache):
         """Time candidate schedules of the precision batch (persistent CTAs x
@@ -234,7 +243,7 @@ class BatchedHMatrices:
         images = [all_images[k] for k in idx]
         rhs = [self.rhs[k] for k in idx]
         orders = [self.orders[k] for k in idx]
-        key = self._tune_key(idx, rhs)
+        key = self._tune_key(idx, rhs) + f"-s{self.pf_seg}"
         path = Path(cache) if cache else Path(os.environ.get("QHMAT_GB300_AUTOTUNE",
                                                              Path.home() / ".cache" / "qhmat_gb300" / "autotune.json"))
         table = {}
@@ -253,7 +262,8 @@ class BatchedHMatrices:
         results = []
         for grid in (sms, sms // 2):
             for row_items in (3.0, 6.0):
-                b = _Batch(images, orders, rhs, [int(v) for v in x_offs[:-1]], self.device, True, grid, row_items)
+                b = _Batch(images, orders, rhs, [int(v) for v in x_offs[:-1]], self.device, True, grid, row_items,
+                           self.pf_seg)
                 s = torch.cuda.current_stream(self.dev)
                 for _ in range(2):
                     b.apply(x, y, s)

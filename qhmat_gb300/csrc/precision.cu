@@ -79,13 +79,16 @@ constexpr int kNMax = 192;        // N of one pass (3 limbs x 64 right-hand side
 constexpr int kBTileBytes = kNMax * 128;   // B operand stage (N rows of 64 f16)
 constexpr int kURawBytes = kPfK * kPfMaxRhs * 4;  // 64 slots of FP32 u
 constexpr int kWaitLimit = 1 << 22;
-// K chunks one accumulation segment spans.  The tensor cores add each MMA's
-// products into the FP32 accumulator with truncation, so the error of an
-// accumulator grows with its number of MMAs (measured: relative error
-// proportional to the chain length); segments of a few chunks are drained
-// into round-to-nearest FP32 registers by the epilogue warps, from two
-// alternating tensor-memory buffers (columns 0 and 256).
-constexpr int kSegChunks = 2;
+// K chunks one accumulation segment spans (a kernel template parameter, SEG,
+// chosen per handle: 2 by default, 1 for matrices whose tolerance asks for
+// it).  The tensor cores add each MMA's products into the FP32 accumulator
+// with truncation, so the error of an accumulator grows with its number of
+// MMAs (measured: relative error proportional to the chain length); segments
+// of a few chunks are drained into round-to-nearest FP32 registers by the
+// epilogue warps, from two alternating tensor-memory buffers (columns 0 and
+// 256).  On the n=32768 x 64 workload: 2 chunks 4.8e-7 relative to the plain
+// form, 1 chunk 2.4e-7 at 4% more time per pass.
+constexpr int kDefaultSegChunks = 2;
 constexpr int kAccStride = 256;
 constexpr int kStatusNonfinite = QH_STATUS_NONFINITE;
 constexpr int kStatusTimeout = QH_STATUS_TIMEOUT;
@@ -435,6 +438,7 @@ __global__ void __launch_bounds__(256) pf_xlimbs_kernel(const double* __restrict
 // ------------------------------------------------------------ column kernel
 
 // Persistent: block g runs column items col_sched[g] .. col_sched[g+1].
+template <int kSegChunks>
 __global__ void __launch_bounds__(ColRoles::kThreads, 1) pf_column_kernel(Arena A, Work W,
                                                                           const __grid_constant__ CUtensorMap xmap,
                                                                           int p, int N, int pu, int* status) {
@@ -635,6 +639,7 @@ __global__ void __launch_bounds__(ColRoles::kThreads, 1) pf_column_kernel(Arena 
 
 // ------------------------------------------------------------ row kernel
 
+template <int kSegChunks>
 __global__ void __launch_bounds__(RowRoles::kThreads, 1) pf_row_kernel(Arena A, Work W,
                                                                        const __grid_constant__ CUtensorMap xmap, int p,
                                                                        int N, int pu, int u_beta, int* status) {
@@ -944,6 +949,7 @@ struct qh_pmatrix {
     void* pinned = nullptr;
     size_t pinned_bytes = 0;
     int host_direct = -1;  // -1: not probed yet
+    int seg = pf::kDefaultSegChunks;  // K chunks per accumulation segment (1 or 2)
     ~qh_pmatrix() {
         int prev = 0;
         cudaGetDevice(&prev);
@@ -1047,10 +1053,21 @@ int pf_pass(const qh_pmatrix* m, const double* x, double* y, int p, long long ld
     pf::pf_xmax_kernel<<<(n + 255) / 256, 64, 0, s>>>(x, ld, n, p, W.ex, status);
     pf::pf_xlimbs_kernel<<<(P.n_ent + 255) / 256, 256, 0, s>>>(x, ld, n, p, P.n_ent, P.N, m->A.perm, W.ex, W.xt);
     mark(1);
-    if (L.n_col_items > 0)
-        pf::pf_column_kernel<<<L.grid, pf::ColRoles::kThreads, pf::kSmemColumn, s>>>(m->A, W, map, p, P.N, P.pu, status);
+    if (L.n_col_items > 0) {
+        if (m->seg == 1)
+            pf::pf_column_kernel<1><<<L.grid, pf::ColRoles::kThreads, pf::kSmemColumn, s>>>(m->A, W, map, p, P.N, P.pu,
+                                                                                           status);
+        else
+            pf::pf_column_kernel<2><<<L.grid, pf::ColRoles::kThreads, pf::kSmemColumn, s>>>(m->A, W, map, p, P.N, P.pu,
+                                                                                           status);
+    }
     mark(2);
-    pf::pf_row_kernel<<<L.grid, pf::RowRoles::kThreads, pf::kSmemRow, s>>>(m->A, W, map, p, P.N, P.pu, L.u_beta, status);
+    if (m->seg == 1)
+        pf::pf_row_kernel<1><<<L.grid, pf::RowRoles::kThreads, pf::kSmemRow, s>>>(m->A, W, map, p, P.N, P.pu, L.u_beta,
+                                                                                  status);
+    else
+        pf::pf_row_kernel<2><<<L.grid, pf::RowRoles::kThreads, pf::kSmemRow, s>>>(m->A, W, map, p, P.N, P.pu, L.u_beta,
+                                                                                  status);
     mark(3);
     const long long total = (long long)n * p;
     pf::pf_combine_kernel<<<unsigned((total + 255) / 256), 256, 0, s>>>(m->A.perm, m->tile_part0, W.part, y, ld, n,
@@ -1099,9 +1116,10 @@ int pf_upload(const HostMatrix& hm, int device, int grid, double row_items_per_c
     if (e == cudaSuccess) e = cudaMalloc(&m->tile_part0, 4 * m->L.tile_part0.size());
     if (e == cudaSuccess)
         e = cudaMemcpy(m->tile_part0, m->L.tile_part0.data(), 4 * m->L.tile_part0.size(), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(pf::pf_column_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, pf::kSmemColumn);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(pf::pf_row_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, pf::kSmemRow);
+    for (auto* k : {pf::pf_column_kernel<1>, pf::pf_column_kernel<2>})
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, pf::kSmemColumn);
+    for (auto* k : {pf::pf_row_kernel<1>, pf::pf_row_kernel<2>})
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, pf::kSmemRow);
     if (e != cudaSuccess) {
         delete m;
         return cuda_err(e, "precision form upload");
@@ -1181,6 +1199,15 @@ int qh_pmatrix_stats(const qh_pmatrix* m, qh_pstats* out) {
     out->mma_col_elements = L.mma_col;
     out->mma_row_elements = L.mma_row;
     out->launches_per_pass = 4 + (L.n_col_items > 0 ? 1 : 0);
+    out->segment_chunks = uint64_t(m->seg);
+    return QH_OK;
+}
+
+int qh_pmatrix_set_segment_chunks(qh_pmatrix* m, int chunks) {
+    if (!m) return set_error(QH_EINVAL, "null matrix handle");
+    if (chunks != 1 && chunks != 2) return set_error(QH_EINVAL, "segment chunks must be 1 or 2");
+    std::lock_guard<std::mutex> lock(m->mu);
+    m->seg = chunks;
     return QH_OK;
 }
 

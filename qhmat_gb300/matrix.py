@@ -300,6 +300,17 @@ class PrecisionHMatrix:
         return int(self._lib.qh_pworkspace_bytes(self._h, rhs))
 
     @property
+    def segment_chunks(self) -> int:
+        """K chunks per FP32 accumulation segment: 2 (default, faster) or 1
+        (half the error: the tensor cores truncate as they accumulate)."""
+        return self._stats["segment_chunks"]
+
+    @segment_chunks.setter
+    def segment_chunks(self, chunks: int) -> None:
+        raise_for(self._lib.qh_pmatrix_set_segment_chunks(self._h, int(chunks)))
+        self._stats["segment_chunks"] = int(chunks)
+
+    @property
     def host_direct(self) -> bool:
         """True when NumPy applies read x and write y in host memory in place
         (the device walks the host's page tables), False when staged."""
@@ -377,10 +388,22 @@ def choose_form(plain: "HMatrix", pf: PrecisionHMatrix, *, probes: int = 8, marg
     forms to ``probes`` seeded N(0, 1) columns and choose the precision form
     when the worst column's gate ratio (see :func:`precision_gate`) is at most
     ``margin`` -- a calibration, since the FP32 rounding of the precision
-    form scales with the data and the gate with the matrix's bound."""
+    form scales with the data and the gate with the matrix's bound.  The
+    precision form is tried with two-chunk accumulation segments, then, if
+    that misses the margin, with one-chunk segments (half the error, ~4% more
+    time); the handle keeps the setting that passed (two when neither did)."""
     x = np.random.default_rng(seed).standard_normal((plain.order, probes))
-    gate = precision_gate(pf.matmul(x), plain.matmul(x), x, plain.reconstruction_bound)
+    y_plain = plain.matmul(x)
+    gate = precision_gate(pf.matmul(x), y_plain, x, plain.reconstruction_bound)
+    if gate["worst_ratio"] > margin:
+        pf.segment_chunks = 1
+        fine = precision_gate(pf.matmul(x), y_plain, x, plain.reconstruction_bound)
+        if fine["worst_ratio"] <= margin:
+            gate = fine
+        else:
+            pf.segment_chunks = 2
     gate["form"] = "precision" if gate["worst_ratio"] <= margin else "plain"
+    gate["segment_chunks"] = pf.segment_chunks
     gate["margin"] = margin
     return gate
 

@@ -98,6 +98,28 @@ def test_host_buffers_match_device_buffers(cuda_device):
     assert pm.host_direct in (True, False)
 
 
+def test_one_chunk_segments_are_closer_to_the_plain_form(cuda_device):
+    """Accumulation segments of one K chunk (the setting calibration falls
+    back to for tight tolerances) are deterministic, pass the gate and are no
+    farther from the plain form than the default two-chunk segments; other
+    settings are rejected."""
+    data, _ = golden("ragged300")
+    h = HMatrix.from_bytes(data)
+    pm = PrecisionHMatrix.from_bytes(data)
+    x = np.random.default_rng(21).standard_normal((300, 40))
+    y_plain = h.matmul(x)
+    assert pm.segment_chunks == 2
+    e2 = rel_err(pm.matmul(x), y_plain)
+    pm.segment_chunks = 1
+    y1 = pm.matmul(x)
+    assert np.array_equal(y1, pm.matmul(x))
+    assert rel_err(y1, y_plain) <= max(e2, 1e-9) * 1.5
+    assert precision_gate(y1, y_plain, x, h.reconstruction_bound)["passes"]
+    with pytest.raises(ValueError):
+        pm.segment_chunks = 3
+    assert pm.segment_chunks == 1
+
+
 def test_precision_form_large_blocks_p64(cuda_device):
     """1-D n = 4096, -log(r + 1e-3), tolerance 1e-6: blocks up to 1024 columns,
     64 right-hand sides in one pass."""
