@@ -305,6 +305,14 @@ PfLayout build_pf_layout(const HostMatrix& m, int grid, double row_items_per_cta
         L.tile_part0[size_t(n_tiles)] = part;
         L.n_parts = part;
     }
+    // the row item holding each low-rank slot (for the items' own u bounds)
+    std::vector<int32_t> item_of_slot(size_t(L.n_slots), -1);
+    for (size_t i = 0; i < row_items.size(); ++i)
+        for (int32_t c = row_items[i].chunk0; c < row_items[i].chunk0 + row_items[i].nchunks; ++c)
+            if (chunks[size_t(c)].kind == 0)
+                for (int32_t sl = chunks[size_t(c)].b; sl < chunks[size_t(c)].b + kPfK && sl < L.n_slots; ++sl)
+                    item_of_slot[size_t(sl)] = int32_t(i);
+    std::vector<double> item_ubound(row_items.size(), 0.0);
 
     // ---- column side: components grouped by column range, widest first, 128 per item
     std::map<std::pair<uint64_t, uint64_t>, std::vector<int32_t>> groups;
@@ -354,10 +362,15 @@ PfLayout build_pf_layout(const HostMatrix& m, int grid, double row_items_per_cta
                 pc.scale = m.left_scale[g] * m.right_scale[g];
                 // |u_j| <= |s^P s^Q| ||c^Q_j||_1 max|x|; the row side scales u by
                 // 256^(P-1) of its chunk: track the largest such bound
-                int pdmax = 1;
-                for (int32_t dw : comp_dests[size_t(ci)]) pdmax = std::max(pdmax, (dw >> 28) + 1);
-                const double ub = std::fabs(pc.scale) * l1 * std::ldexp(1.0, 8 * (pdmax - 1));
-                if (ub > 0.0 && std::isfinite(ub)) ubound = std::max(ubound, ub);
+                // (overall, and per row item over the slots it holds)
+                const double ub0 = std::fabs(pc.scale) * l1;
+                for (int32_t dw : comp_dests[size_t(ci)]) {
+                    const double ub = ub0 * std::ldexp(1.0, 8 * (dw >> 28));
+                    if (!(ub > 0.0 && std::isfinite(ub))) continue;
+                    ubound = std::max(ubound, ub);
+                    const int32_t item = item_of_slot[size_t(dw & 0x0FFFFFFF)];
+                    if (item >= 0) item_ubound[size_t(item)] = std::max(item_ubound[size_t(item)], ub);
+                }
                 pc.dest0 = int32_t(dests.size());
                 pc.ndest = int32_t(comp_dests[size_t(ci)].size());
                 dests.insert(dests.end(), comp_dests[size_t(ci)].begin(), comp_dests[size_t(ci)].end());
@@ -373,6 +386,8 @@ PfLayout build_pf_layout(const HostMatrix& m, int grid, double row_items_per_cta
     // 2^u_beta > every |u_j| 256^(P-1) / max|x| (with a factor 2 of room for
     // the FP32 rounding of u)
     L.u_beta = ubound > 0.0 ? std::ilogb(ubound) + 2 : 0;
+    for (size_t i = 0; i < row_items.size(); ++i)
+        row_items[i].u_beta = item_ubound[i] > 0.0 ? std::ilogb(item_ubound[i]) + 2 : L.u_beta;
     L.n_col_items = int32_t(col_items.size());
     L.n_row_items = int32_t(row_items.size());
     L.n_dests = int32_t(dests.size());

@@ -63,10 +63,12 @@ static_assert(sizeof(PfComp) == 16, "PfComp layout");
 // A row-side work item: K split `h` of the 128-row tile `tile` (clustered
 // rows [row0, row0 + rows)), chunks [chunk0, chunk0 + nchunks); its FP64
 // partial sums go to partial slot `part`.  Dense limb tiles of the tile are
-// scaled by 2^-dense_exp.
+// scaled by 2^-dense_exp.  u_beta: the item's own bound on its slots' u (as
+// PfLayout::u_beta, over this item's slots only), so that the limbs of U'
+// carry full precision whatever the other items' magnitudes.
 struct PfRowItem {
     int32_t tile, row0, rows, part;
-    int32_t chunk0, nchunks, dense_exp, pad;
+    int32_t chunk0, nchunks, dense_exp, u_beta;
 };
 static_assert(sizeof(PfRowItem) == 32, "PfRowItem layout");
 
@@ -97,7 +99,8 @@ struct PfLayout {
     int32_t grid = 0;  // persistent CTAs the schedules are built for
     // Layout-time bound on the row side's u operand: for every component j and
     // every destination chunk of P planes, |u_j| 256^(P-1) < 2^u_beta max|x|,
-    // so the per-column scale of U' needs no pass over u.
+    // so the per-column scale of U' needs no pass over u.  The largest of the
+    // row items' own bounds (PfRowItem::u_beta <= u_beta).
     int32_t u_beta = 0;
     double bound = 0;
     std::vector<uint8_t> arena;

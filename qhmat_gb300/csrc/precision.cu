@@ -312,24 +312,29 @@ __device__ __forceinline__ void convert_plane(const uint8_t* raw, uint8_t* tile,
     }
 }
 
+// 2^k as a float, k clamped to the normal range [-126, 127].
+__device__ __forceinline__ float pow2f_clamped(int k) { return __int_as_float((127 + max(-126, min(127, k))) << 23); }
+constexpr int kZeroColumn = -(1 << 20);  // ku of a right-hand side that is all zero
+
 __device__ __forceinline__ uint32_t pack_h2(__half a, __half b) {
     return uint32_t(__half_as_ushort(a)) | (uint32_t(__half_as_ushort(b)) << 16);
 }
 
 // U of 64 slots (FP32, row stride pu) -> the f16 B tile: row 3r + l holds limb
-// l of u' = u 2^k[r] 256^(P-1) for the 64 slots of a chunk with P planes
-// (slots >= nvalid: 0).  Pairs of slots are split with packed conversions.
+// l of u' = u 2^(ku[r] + dk) 256^(P-1) for the 64 slots of a chunk with P
+// planes (slots >= nvalid: 0; dk = the layout's u_beta minus the item's).
+// Pairs of slots are split with packed conversions.
 template <int NT>
 __device__ __forceinline__ void convert_u(const float* raw, uint8_t* tile, int p, int pu, int nvalid, int P,
-                                          const float* scale, int ctid) {
-    const float pw = __int_as_float((127 + 8 * (P - 1)) << 23);  // 256^(P-1)
+                                          const int* ku, int dk, int ctid) {
     constexpr int kIters = (8 * kPfMaxRhs + NT - 1) / NT;
 #pragma unroll
     for (int it = 0; it < kIters; ++it) {
         const int idx = ctid + it * NT;
         if (idx >= p * 8) break;
         const int r = idx % p, kg = idx / p;
-        const float sc = scale[r] * pw;
+        // 2^(ku + dk) 256^(P-1): the column's scale on this item's bound
+        const float sc = ku[r] == kZeroColumn ? 0.0f : pow2f_clamped(ku[r] + dk + 8 * (P - 1));
         float v[8];
 #pragma unroll
         for (int s = 0; s < 8; ++s) {
@@ -364,10 +369,9 @@ struct Shared {
     uint32_t tmem;
     int abort_flag;
     int ex[kPfMaxRhs];
-    int ku[kPfMaxRhs];      // row kernel: U' = u 2^ku
-    float uscale[kPfMaxRhs];
+    int ku[kPfMaxRhs];      // row kernel: U' = u 2^(ku + u_beta - item's u_beta); kZeroColumn for x = 0
     float fxscale[kPfMaxRhs];  // column kernel: 2^(24 + E_r - 1037)
-    float flscale[kPfMaxRhs];  // row kernel: 2^-ku (low-rank sums)
+    float flitem[4][kPfMaxRhs];  // row kernel, per drain warp: the current item's 2^-(ku + ...) (low-rank sums)
     float fdscale[kPfMaxRhs];  // row kernel: 2^(E_r - 1037) (dense sums, times 2^dense_exp)
 };
 
@@ -660,11 +664,9 @@ __global__ void __launch_bounds__(RowRoles::kThreads, 1) pf_row_kernel(Arena A, 
         S.ex[tid] = E;
         S.fdscale[tid] = E ? ldexpf(1.0f, max(-126, min(127, E - 1037))) : 0.0f;
         // U' = u 256^(P-1) 2^k < 2^15 by the layout-time bound
-        // |u| 256^(P-1) < 2^(u_beta + E - 1022)
-        const int k = E ? max(-126, min(127, 1037 - E - u_beta)) : 0;
-        S.ku[tid] = k;
-        S.uscale[tid] = E ? ldexpf(1.0f, k) : 0.0f;
-        S.flscale[tid] = E ? ldexpf(1.0f, -k) : 0.0f;
+        // |u| 256^(P-1) < 2^(u_beta + E - 1022); an item applies its own,
+        // smaller bound: k + (u_beta - the item's u_beta)
+        S.ku[tid] = E ? 1037 - E - u_beta : kZeroColumn;
     }
     // B rows 3p .. N-1 of both f16 B stages stay zero (the converters write
     // only rows < 3p; tensor copies of x write zeros there)
@@ -789,8 +791,8 @@ __global__ void __launch_bounds__(RowRoles::kThreads, 1) pf_row_kernel(Arena A, 
                 if (!ok) break;
                 if (C.kind == 0)
                     convert_u<kConvWarps * 32>(reinterpret_cast<const float*>(sm + kOffBRaw + sb * kURawBytes),
-                                               sm + kOffBF16 + sb * kBTileBytes, p, pu, C.nvalid, C.planes, S.uscale,
-                                               ctid);
+                                               sm + kOffBF16 + sb * kBTileBytes, p, pu, C.nvalid, C.planes, S.ku,
+                                               u_beta - I.u_beta, ctid);
                 fence_async_smem();
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&S.b_conv[sb]);
@@ -831,6 +833,10 @@ __global__ void __launch_bounds__(RowRoles::kThreads, 1) pf_row_kernel(Arena A, 
                 for (int g = 0; g < kPfMaxRhs / 16; ++g)
                     if (16 * g < p) tmem_st16(yb + 16 * g, z);
                 tmem_wait_st();
+                // this item's low-rank scales 2^-(ku + u_beta - item's u_beta)
+                for (int r = lane; r < kPfMaxRhs; r += 32)
+                    S.flitem[q][r] = S.ku[r] == kZeroColumn ? 0.0f : pow2f_clamped(-(S.ku[r] + u_beta - I.u_beta));
+                __syncwarp();
             }
             const float dexp = ldexpf(1.0f, max(-126, min(127, I.dense_exp)));
             int c = 0;
@@ -860,7 +866,7 @@ __global__ void __launch_bounds__(RowRoles::kThreads, 1) pf_row_kernel(Arena A, 
                         const float a0 = c0 < 16 ? v0[c0] : (c0 < 32 ? v1[c0 - 16] : v2[c0 - 32]);
                         const float a1 = c1 < 16 ? v0[c1] : (c1 < 32 ? v1[c1 - 16] : v2[c1 - 32]);
                         const float a2 = c2 < 16 ? v0[c2] : (c2 < 32 ? v1[c2 - 16] : v2[c2 - 32]);
-                        const float sc = kind == 0 ? S.flscale[r] : S.fdscale[r] * dexp;
+                        const float sc = kind == 0 ? S.flitem[q][r] : S.fdscale[r] * dexp;
                         y[i] = fmaf((a0 + a1) + a2, sc, y[i]);
                     }
                     tmem_st16(yb + 16 * g, y);
