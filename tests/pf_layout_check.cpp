@@ -135,9 +135,15 @@ int main(int argc, char** argv) {
     std::vector<double> part(size_t(L.n_parts) * kPfM, 0.0);
     std::vector<int> part_seen(size_t(L.n_parts), 0);
     std::vector<int> chunk_seen(size_t(L.n_chunks), 0);
+    double xmax = 0.0;
+    for (int64_t e = 0; e < n; ++e) xmax = std::max(xmax, std::fabs(xc[size_t(e)]));
     for (int32_t it = 0; it < L.n_row_items; ++it) {
         const PfRowItem& I = ri[it];
         ++part_seen[size_t(I.part)];
+        if (I.u_beta > L.u_beta) {
+            std::printf("FAIL row item %d: bound %d above the layout's %d\n", it, I.u_beta, L.u_beta);
+            return 1;
+        }
         for (int c = 0; c < I.nchunks; ++c) {
             const PfRowChunk& C = ch[I.chunk0 + c];
             ++chunk_seen[size_t(I.chunk0 + c)];
@@ -159,6 +165,13 @@ int main(int argc, char** argv) {
                         if (slot_planes[size_t(C.b + k)] != C.planes) {
                             std::printf("FAIL slot %d: dest planes %d, chunk planes %d\n", C.b + k,
                                         slot_planes[size_t(C.b + k)], C.planes);
+                            return 1;
+                        }
+                        // the item's own bound holds for every slot it reads:
+                        // |u| 256^(P-1) < 2^u_beta max|x|
+                        if (std::fabs(U[size_t(C.b + k)]) * std::ldexp(1.0, 8 * (C.planes - 1)) >=
+                            std::ldexp(xmax, I.u_beta)) {
+                            std::printf("FAIL slot %d: |u| above its row item's bound\n", C.b + k);
                             return 1;
                         }
                         part[size_t(I.part) * kPfM + size_t(off + r)] += double(code) * U[size_t(C.b + k)];
