@@ -712,7 +712,14 @@ __global__ void __launch_bounds__(kWarps * 32, QH_COL_CTAS) column_kernel(Arena 
         const int nb = my_units;
         int ik = 0, ip = 0, ic = 0;  // issue cursor
         ColTask di = unit(0);
-        pdl_wait();  // x limbs and exponents of this apply
+        // The first stages' code bytes come from the read-only arena, so they
+        // are fetched while the preceding kernel finishes; their x limbs only
+        // after it has (programmatic dependent launch): deferred copies.
+        bool defer = true;
+        int npend = 0;
+        const void* pend_src[kColStages];
+        uint8_t* pend_dst[kColStages];
+        unsigned pend_bytes[kColStages], pend_slot[kColStages];
         auto issue = [&]() {
             while (ik < nb && di.width == 0) {  // dense units stream nothing
                 if (++ik < nb) di = unit(ik);
@@ -728,7 +735,14 @@ __global__ void __launch_bounds__(kWarps * 32, QH_COL_CTAS) column_kernel(Arena 
                 fence_async_smem();
                 mbar_arrive_expect(bar + slot_i, wbytes + xbytes);
                 bulk_load(slot, A.qcodes + di.off + (long long)(di.chunk0 + ic) * di.stride, wbytes, bar + slot_i);
-                bulk_load(slot + wbytes, W.xq + (long long)ip * n_pad + di.col0 + k0, xbytes, bar + slot_i);
+                const void* xsrc = W.xq + (long long)ip * n_pad + di.col0 + k0;
+                if (defer) {
+                    pend_src[npend] = xsrc, pend_dst[npend] = slot + wbytes;
+                    pend_bytes[npend] = xbytes, pend_slot[npend] = slot_i;
+                    ++npend;
+                } else {
+                    bulk_load(slot + wbytes, xsrc, xbytes, bar + slot_i);
+                }
             }
             ++issued;
             ic += nc;
@@ -747,6 +761,10 @@ __global__ void __launch_bounds__(kWarps * 32, QH_COL_CTAS) column_kernel(Arena 
         ColTask dc = di;
 #pragma unroll 1
         for (int s = 0; s < kColStages - 1; ++s) issue();
+        pdl_wait();  // x limbs and exponents of this apply
+        defer = false;
+        if (lane == 0)
+            for (int i = 0; i < npend; ++i) bulk_load(pend_dst[i], pend_src[i], pend_bytes[i], bar + pend_slot[i]);
         const int xe0 = W.xe[0];
         // this lane's component scale and first B row record, loaded when a
         // unit starts (the record by an asynchronous copy into shared
@@ -975,8 +993,15 @@ __global__ void __launch_bounds__(kWarps * 32, QH_ROW_CTAS) row_kernel(Arena A, 
         int ik = 0, ip = 0, is = 0, isb = 0, ii = 0;
         long long ioff = 0;
         RowDesc di = load_rdesc(my_units_p);
-        pdl_wait();  // B rows of this apply
         if (lane < 2 && lane + 1 < nb) prefetch_l1(my_units_p + lane + 1);
+        // The first stages' code bytes come from the read-only arena, so they
+        // are fetched while the column kernel finishes; their B rows only
+        // after it has (programmatic dependent launch): deferred copies.
+        bool defer = true;
+        int npend = 0;
+        const void* pend_src[kRowStages];
+        uint8_t* pend_dst[kRowStages];
+        unsigned pend_bytes[kRowStages], pend_slot[kRowStages];
         auto load_steps = [&](const RowDesc& d, int base) {
             return base + lane < d.nsteps ? __ldg(A.row_steps + d.step0 + base + lane) : 0u;
         };
@@ -1000,7 +1025,14 @@ __global__ void __launch_bounds__(kWarps * 32, QH_ROW_CTAS) row_kernel(Arena A, 
                 fence_async_smem();
                 mbar_arrive_expect(bar + slot_i, unsigned(cbytes) + lbytes);
                 bulk_load(slot, A.pcodes + di.code_off + ioff, unsigned(cbytes), bar + slot_i);
-                bulk_load(slot + cbytes, W.blimb + (long long)ip * n_slots + di.slot0 + 32 * ii, lbytes, bar + slot_i);
+                const void* bsrc = W.blimb + (long long)ip * n_slots + di.slot0 + 32 * ii;
+                if (defer) {
+                    pend_src[npend] = bsrc, pend_dst[npend] = slot + cbytes;
+                    pend_bytes[npend] = lbytes, pend_slot[npend] = slot_i;
+                    ++npend;
+                } else {
+                    bulk_load(slot + cbytes, bsrc, lbytes, bar + slot_i);
+                }
             }
             ++issued;
             ++is;
@@ -1032,6 +1064,10 @@ __global__ void __launch_bounds__(kWarps * 32, QH_ROW_CTAS) row_kernel(Arena A, 
         RowDesc dc = di;
 #pragma unroll 1
         for (int s = 0; s < kRowStages - 1; ++s) issue();
+        pdl_wait();  // B rows of this apply
+        defer = false;
+        if (lane == 0)
+            for (int i = 0; i < npend; ++i) bulk_load(pend_dst[i], pend_src[i], pend_bytes[i], bar + pend_slot[i]);
         uint32_t csteps = load_steps(dc, 0);
         int cinfo = load_info(dc, 0);
         float D[4][4];
