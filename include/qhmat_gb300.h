@@ -242,6 +242,15 @@ typedef struct {
 /* Parse a QHMAT001 image (the checks and messages of qh_matrix_from_qhmat)
  * and upload the precision-form layout to `device`. */
 QH_API int qh_pmatrix_from_qhmat(const void* bytes, size_t len, int device, qh_pmatrix** out);
+/* Device bytes the resident arenas of a QHMAT001 image will take, without
+ * touching a device: the plain form's (qh_stats.device_bytes of
+ * qh_matrix_from_qhmat) and the precision form's (qh_pstats.device_bytes of
+ * qh_pmatrix_from_qhmat on a device of `sms` multiprocessors, whose
+ * schedules it sizes); either output may be NULL.  Parses the image with the
+ * checks and messages of qh_matrix_from_qhmat.  For admission control before
+ * an upload.  No reference counterpart. */
+QH_API int qh_qhmat_device_bytes(const void* bytes, size_t len, int sms, uint64_t* plain_bytes,
+                                 uint64_t* precision_bytes);
 QH_API void qh_pmatrix_destroy(qh_pmatrix* m);
 QH_API int qh_pmatrix_stats(const qh_pmatrix* m, qh_pstats* out);
 /* K chunks (of 64 entries) that one FP32 accumulation segment spans: 2 (the

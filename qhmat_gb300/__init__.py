@@ -7,7 +7,7 @@ once and applied by hand-written sm_103a kernels through the C ABI declared in
 """
 
 from ._lib import LIB_PATH, load_library
-from .matrix import HMatrix, NativeHMatrix, PrecisionHMatrix, choose_form, precision_gate
+from .matrix import HMatrix, NativeHMatrix, PrecisionHMatrix, choose_form, precision_gate, qhmat_device_bytes
 
 cuda_built = True
 

@@ -94,6 +94,8 @@ def load_library() -> C.CDLL:
     lib.qh_pworkspace_bytes.argtypes = [vp, sz]
     lib.qh_pmatmul_device.restype = i32
     lib.qh_pmatmul_device.argtypes = [vp, vp, vp, sz, vp, sz, vp, vp]
+    lib.qh_qhmat_device_bytes.restype = i32
+    lib.qh_qhmat_device_bytes.argtypes = [C.c_char_p, sz, C.c_int, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
     lib.qh_pmatrix_set_segment_chunks.restype = i32
     lib.qh_pmatrix_set_segment_chunks.argtypes = [vp, C.c_int]
     lib.qh_pmatmul_host.restype = i32

@@ -1182,6 +1182,18 @@ int qh_pmatrix_from_batch(const void* const* images, const size_t* lens, size_t 
 
 void qh_pmatrix_destroy(qh_pmatrix* m) { delete m; }
 
+int qh_qhmat_device_bytes(const void* bytes, size_t len, int sms, uint64_t* plain_bytes, uint64_t* precision_bytes) {
+    if (!plain_bytes && !precision_bytes) return set_error(QH_EINVAL, "no output requested");
+    if (!bytes && len) return set_error(QH_EINVAL, "image pointer is null");
+    if (sms < 1) return set_error(QH_EINVAL, "the SM count must be positive");
+    return guarded_pf([&] {
+        HostMatrix hm = parse_qhmat(static_cast<const uint8_t*>(bytes), len);
+        if (plain_bytes) *plain_bytes = uint64_t(build_layout(hm).sec.total);
+        if (precision_bytes) *precision_bytes = uint64_t(build_pf_layout(hm, sms, 0.0).sec.total);
+        return int(QH_OK);
+    });
+}
+
 size_t qh_pworkspace_bytes(const qh_pmatrix* m, size_t rhs) {
     return m && rhs ? pf_plan(m->L, rhs).total : 0;
 }

@@ -408,5 +408,17 @@ def choose_form(plain: "HMatrix", pf: PrecisionHMatrix, *, probes: int = 8, marg
     return gate
 
 
+def qhmat_device_bytes(data: bytes, *, sms: int, precision: bool = True) -> tuple[int, int]:
+    """(plain-form, precision-form) device bytes of a QHMAT001 image's
+    resident arenas, computed on the host without a device (the precision
+    form's for a device of ``sms`` multiprocessors; 0 when ``precision`` is
+    False).  Raises as ``HMatrix.from_bytes`` does for a corrupt image."""
+    lib = load_library()
+    plain, pf = C.c_uint64(), C.c_uint64()
+    raise_for(lib.qh_qhmat_device_bytes(bytes(data), len(data), int(sms), C.byref(plain),
+                                        C.byref(pf) if precision else None))
+    return int(plain.value), int(pf.value) if precision else 0
+
+
 def cuda_built() -> bool:
     return bool(load_library().qh_cuda_built())

@@ -38,7 +38,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from ._lib import load_library, raise_for
-from .matrix import HMatrix, PrecisionHMatrix
+from .matrix import HMatrix, PrecisionHMatrix, qhmat_device_bytes
 
 
 class AdmissionError(RuntimeError):
@@ -126,30 +126,43 @@ class ServingPool:
 
     def admit(self, key, data: bytes, *, columns: int = 0) -> Resident:
         """Upload a QHMAT001 image; optionally attach pinned input/output
-        buffers of ``columns`` columns for requests.  Raises AdmissionError
-        (nothing stays resident) if it cannot fit."""
+        buffers of ``columns`` columns for requests.  The image's device
+        footprint is computed on the host first (the layouts the upload will
+        build) and reserved -- evicting idle matrices if needed -- before any
+        device allocation, so the budget holds throughout.  Raises
+        AdmissionError (nothing becomes resident, nothing is evicted) if it
+        cannot fit; a corrupt image raises before anything is reserved."""
         import torch
 
-        plain = HMatrix.from_bytes(data, device=self.device)  # parses and validates (corrupt images raise)
-        pf = None
+        sms = torch.cuda.get_device_properties(self.device).multi_processor_count
+        plain_b, pf_b = qhmat_device_bytes(data, sms=sms, precision=self.precision)
+        nbytes = plain_b + pf_b
+        with self._lock:
+            victims = self.admission.reserve(key, nbytes)
+            for v in victims:
+                self._drop(v)
+            self.admission.commit(key, nbytes)
+        plain = pf = None
         form = "plain"
-        nbytes = plain.stats["device_bytes"]
         try:
+            plain = HMatrix.from_bytes(data, device=self.device)
             if self.precision:
                 pf = PrecisionHMatrix.from_bytes(data, device=self.device)
-                nbytes += pf.stats["device_bytes"]
-                choice = plain.attach_precision(pf)
-                form = choice["form"]
-            with self._lock:
-                victims = self.admission.reserve(key, nbytes)
-                for v in victims:
-                    self._drop(v)
-                self.admission.commit(key, nbytes)
+                form = plain.attach_precision(pf)["form"]
         except Exception:
             if pf is not None:
                 pf.close()
-            plain.close()
+            if plain is not None:
+                plain.close()
+            with self._lock:
+                self.admission.release(key)
             raise
+        actual = plain.stats["device_bytes"] + (pf.stats["device_bytes"] if pf is not None else 0)
+        if actual != nbytes:  # the same layouts: equal by construction; keep the books exact regardless
+            with self._lock:
+                self.admission.release(key)
+                self.admission.commit(key, actual)
+            nbytes = actual
         r = Resident(key, plain, pf, form, nbytes)
         if columns:
             n = plain.order

@@ -60,3 +60,20 @@ def test_tolerance_escalation_reaches_a_feasible_tolerance():
     assert bench.build_spec(spec, 1, checksum=O.fnv1a64)[0] == data
     m = O.OracleMatrix(data)
     assert m.order == 600
+
+
+def test_device_bytes_query_needs_no_device():
+    """The admission size query parses the image and builds the layouts on
+    the host (no device): positive sizes, the precision form's only when
+    asked for, and the loader's errors for a corrupt image."""
+    from conftest import golden
+    from qhmat_gb300 import qhmat_device_bytes
+
+    data, _ = golden("cfg1")
+    plain, pf = qhmat_device_bytes(data, sms=152)
+    assert plain > 0 and pf > 0
+    assert qhmat_device_bytes(data, sms=152, precision=False) == (plain, 0)
+    with pytest.raises((ValueError, RuntimeError)):
+        qhmat_device_bytes(data[:100], sms=152)
+    with pytest.raises(ValueError, match="SM count"):
+        qhmat_device_bytes(data, sms=0)

@@ -107,3 +107,20 @@ def test_cancel_and_corrupt_upload_and_refusal(cuda_device):
     with pytest.raises(AdmissionError):
         small.admit("m", data)
     assert small.used_bytes == 0
+
+
+def test_device_bytes_query_matches_uploads(cuda_device):
+    """Admission reserves what the host-side size query reports before any
+    upload; it must equal what the uploaded handles report."""
+    import torch
+
+    from qhmat_gb300 import HMatrix, PrecisionHMatrix, qhmat_device_bytes
+
+    for name in ("cfg1", "ragged300"):
+        data, _ = golden(name)
+        h = HMatrix.from_bytes(data)
+        pm = PrecisionHMatrix.from_bytes(data)
+        sms = torch.cuda.get_device_properties(0).multi_processor_count
+        assert qhmat_device_bytes(data, sms=sms) == (h.stats["device_bytes"], pm.stats["device_bytes"])
+        h.close()
+        pm.close()
