@@ -118,6 +118,19 @@ class _Batch:
             self.h = C.c_void_p()
 
 
+def batch_forms(ratio2, ratio1, rhs, margin: float = 0.5):
+    """The precision batch's segment length and each matrix's form, from the
+    calibration's worst-column gate ratios with two-chunk (``ratio2``) and
+    one-chunk (``ratio1``) accumulation segments: one-chunk segments for the
+    whole precision batch when some matrix passes only with them, and then
+    every matrix judged at that setting; a matrix with fewer than two columns
+    stays plain (the precision form serves multi-column applies)."""
+    need_fine = any(r2 > margin and r1 <= margin and p >= 2 for r2, r1, p in zip(ratio2, ratio1, rhs))
+    seg = 1 if need_fine else 2
+    ratios = ratio1 if seg == 1 else ratio2
+    return seg, ["precision" if r <= margin and p >= 2 else "plain" for r, p in zip(ratios, rhs)]
+
+
 def _bucket(v, edges):
     for e in edges:
         if v <= e:
@@ -228,11 +241,9 @@ class BatchedHMatrices:
                 g = precision_gate(y[a:b_].reshape(shape), outs[0][a:b_].reshape(shape), xh[a:b_].reshape(shape),
                                    self.bounds[k])
                 ratios[seg].append(g["worst_ratio"])
-        need_fine = any(r2 > 0.5 and r1 <= 0.5 and self.rhs[k] >= 2
-                        for k, (r2, r1) in enumerate(zip(ratios[2], ratios[1])))
-        self.pf_seg = 1 if need_fine else 2
+        self.pf_seg, forms = batch_forms(ratios[2], ratios[1], self.rhs)
         self.calibration = ratios[self.pf_seg]
-        return ["precision" if r <= 0.5 and self.rhs[k] >= 2 else "plain" for k, r in enumerate(self.calibration)]
+        return forms
 
     def _autotune(self, idx, all_images, cache):
         """Time candidate schedules of the precision batch (persistent CTAs x
