@@ -919,7 +919,7 @@ def run_serving(args):
     for j, mid in enumerate((6000.0, 10000.0, 14000.0)):
         _, by_rate[str(int(mid))] = served_phase(mid, 43 + j)
     engine.stop(drain=True, timeout=120.0)
-    base_full = plain_phase(20000.0, 41, float(os.environ.get("QHMAT_GB300_SERVE_BASELINE_S", "20")))
+    base_full = plain_phase(20000.0, 41, float(os.environ.get("QHMAT_GB300_SERVE_PLAIN_S", "20")))
     base_low = plain_phase(low_rate, 42, 60.0)
     served = full
     rhs_per_s = full["rhs_per_s"]
